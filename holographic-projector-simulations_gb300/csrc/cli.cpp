@@ -1,0 +1,473 @@
+// cli.cpp -- `holo`, flag- and file-compatible with the reference executable.
+//
+// Short options are the reference's getopt string (cuda/input.h:83) with its
+// defaults (cuda/input.h:48-79); the help text follows cuda/input.h:7-39.
+// File mode (-f dir) reads x0_amp.dat, x0_phase.dat, u0.dat, v0.dat and, with
+// -F, w0_0.dat (falling back to the reference's w0.dat, cuda/main.cu:90) and
+// writes y0_* / v0.dat and z0_0_* / w0_0.dat plus out.json into dir
+// (cuda/main.cu:213-221).  Unlike the reference, -F projects z from the
+// normalised projector field y at v onto w (the x -> y -> z chain); --ref-compat
+// reproduces the reference's -F (z from x at u onto v, cuda/main.cu:219).
+// Without -f the generated-data mode of cuda/main.cu:120-199 runs.
+//
+// Long options added here: --lambda, --precision fp64|split32, --mc SUB,
+// --seed S, --mc-block B, --amplitude-only (PROJECT_PHASE=0), --reference-distance,
+// --ref-compat, --out DIR (generated mode, default ../tmp/ as the reference), --device.
+//
+// Exit codes: 0 success; 2 bad arguments or files; 4 non-finite output (the
+// reference's check_complex exit, cuda/util.h:54-60); 3 a library error.
+#include <curand.h>
+#include <getopt.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include <string>
+#include <vector>
+
+#include "holo.h"
+#include "io.h"
+
+namespace {
+
+constexpr int kNSqrt = 512;  // N_sqrt (cuda/macros.h:8)
+constexpr double kTwoPi = 2 * M_PI;
+
+template <typename T>
+struct Range {
+  T min, max;
+};
+
+struct Params {
+  size_t planes_obj = 1, planes_projection = 1;
+  size_t n_obj = 1, n_projector = (size_t)kNSqrt * kNSqrt, n_projection = (size_t)kNSqrt * kNSqrt;
+  bool n_projector_set = false;
+  double aspect_projector = 1.0, aspect_projection = 1.0;
+  Range<double> off_x{0.0, 0.0}, off_y{0.0, 0.0}, off_z{0.35, 0.25};
+  Range<double> obj_width{1e-3, 1e-3};
+  Range<double> projector_width{kNSqrt * 7e-6, kNSqrt * 7e-6};
+  Range<double> projection_width{1e-3 * 1.2, 1e-3 * 1.2};
+  Range<double> projection_z{0.0, 0.0};
+  int algorithm = 2;
+  bool quadrant = false, randomize = false;
+  int streams = 8;
+  std::string files;
+  bool projection = false;
+  // added
+  double lambda = 0.65e-6;  // the reference's compile-time default LAMBDA (cuda/macros.h:23-25)
+  int precision = HOLO_FP64;
+  int mc_sub = 0;
+  uint64_t seed = 0;
+  int mc_block = 256;
+  bool amplitude_only = false;
+  double reference_distance = 0.25;  // DISTANCE_REFERENCE_WAVE (cuda/macros.h:26-28)
+  bool ref_compat = false;
+  std::string out_dir = "../tmp/";
+  int device = 0;
+};
+
+void show_help(const char *p) {
+  printf(
+      "Usage %s [OPTION]...\n"
+      "Note: for each attribute, if .max is not provided it defaults to the corresponding .min.\n"
+      "\t -h       \tShow help. \n"
+      "\n\tUse external data (optional)\n"
+      "\t -f {dir} \t Read input files from `dir`: `x0_amp.dat, x0_phase.dat, u0.dat, v0.dat`."
+      " These files should be binary arrays representing double-precision floating-point numbers.\n"
+      "\t-F        \t Compute projection distribution (w0_0.dat, or w0.dat) w.r.t. the projector (v).\n"
+      "\n\tPerformance parameters (accepted for compatibility; kernels are tuned automatically)\n"
+      "\t-s        \tSet number of streams.\n"
+      "\t-t, -T    \tSet number of source, target datapoints per thread.\n"
+      "\t-b, -B    \tSet CUDA blockDim .x, .y.\n"
+      "\t-g, -G    \tSet CUDA gridDim .x, .y.\n"
+      "\t-p        \tSelect algorithm 1, 2 or 3 (all map to the same brute-force sum).\n"
+      "\n\tGenerate data (used if `-f {dir}` is not supplied).\n"
+      "\t-X, -Z    \tSet number of input, projection planes.\n"
+      "\t-x, -y, -z\tSet number of input, projector, projection datapoints per plane.\n"
+      "\t-a, -A    \tSet aspect ratio for projector, projection.\n"
+      "\t-u, -U    \tSet .min, .max offset in x-dimension for input objects.\n"
+      "\t-v, -V    \tSet .min, .max offset in y-dimension for input objects.\n"
+      "\t-w, -W    \tSet .min, .max offset in z-dimension for input objects.\n"
+      "\t-o, -O    \tSet .min, .max object width.\n"
+      "\t-l, -L    \tSet .min, .max projector width.\n"
+      "\t-n, -N    \tSet .min, .max projection width.\n"
+      "\t-m, -M    \tSet .min, .max projection offset in z-dimension.\n"
+      "\t-q        \tLimit projection to a single quadrant.\n"
+      "\t-r        \tRandomize projector pixel positions.\n"
+      "\n\tRuntime options (compile-time macros in the reference)\n"
+      "\t--lambda L            \tWavelength in m (default 0.65e-6)\n"
+      "\t--precision P         \tfp64 (default, the reference's arithmetic) or split32\n"
+      "\t--amplitude-only      \tAmplitude-only projector with a reference wave (PROJECT_PHASE=0)\n"
+      "\t--reference-distance D\tDistance of the reference wave source (default 0.25 m)\n"
+      "\t--mc SUB [--seed S] [--mc-block B]\tMonte Carlo estimator: 1/SUB of the sources per block\n"
+      "\t--ref-compat          \tReproduce the reference's -F (z from x at u onto v)\n"
+      "\t--out DIR             \tOutput directory of the generated mode (default ../tmp/)\n"
+      "\t--device D            \tCUDA device\n"
+      "\n",
+      p);
+}
+
+bool parse(int argc, char **argv, Params *p, int *exit_code) {
+  enum { O_LAMBDA = 1000, O_PREC, O_MC, O_SEED, O_MCB, O_AMP, O_REFD, O_COMPAT, O_OUT, O_DEV };
+  static struct option longopts[] = {{"lambda", required_argument, 0, O_LAMBDA},
+                                     {"precision", required_argument, 0, O_PREC},
+                                     {"mc", required_argument, 0, O_MC},
+                                     {"seed", required_argument, 0, O_SEED},
+                                     {"mc-block", required_argument, 0, O_MCB},
+                                     {"amplitude-only", no_argument, 0, O_AMP},
+                                     {"reference-distance", required_argument, 0, O_REFD},
+                                     {"ref-compat", no_argument, 0, O_COMPAT},
+                                     {"out", required_argument, 0, O_OUT},
+                                     {"device", required_argument, 0, O_DEV},
+                                     {"help", no_argument, 0, 'h'},
+                                     {0, 0, 0, 0}};
+  int ch;
+  while ((ch = getopt_long(argc, argv,
+                           "X:Z:x:y:z:a:A:u:U:v:V:w:W:o:O:l:L:n:N:m:M:p:qrs:t:T:b:B:g:G:f:Fh",
+                           longopts, nullptr)) != -1) {
+    switch (ch) {
+      case 'X': p->planes_obj = strtol(optarg, 0, 10); break;
+      case 'Z': p->planes_projection = strtol(optarg, 0, 10); break;
+      case 'x': p->n_obj = strtol(optarg, 0, 10); break;
+      case 'y': p->n_projector = strtol(optarg, 0, 10); p->n_projector_set = true; break;
+      case 'z': p->n_projection = strtol(optarg, 0, 10); break;
+      case 'a': p->aspect_projector = strtod(optarg, 0); break;
+      case 'A': p->aspect_projection = strtod(optarg, 0); break;
+      case 'u': p->off_x.min = p->off_x.max = strtod(optarg, 0); break;
+      case 'U': p->off_x.max = strtod(optarg, 0); break;
+      case 'v': p->off_y.min = p->off_y.max = strtod(optarg, 0); break;
+      case 'V': p->off_y.max = strtod(optarg, 0); break;
+      case 'w': p->off_z.min = p->off_z.max = strtod(optarg, 0); break;
+      case 'W': p->off_z.max = strtod(optarg, 0); break;
+      case 'o': p->obj_width.min = p->obj_width.max = strtod(optarg, 0); break;
+      case 'O': p->obj_width.max = strtod(optarg, 0); break;
+      case 'l': p->projector_width.min = p->projector_width.max = strtod(optarg, 0); break;
+      case 'L': p->projector_width.max = strtod(optarg, 0); break;
+      case 'n': p->projection_width.min = p->projection_width.max = strtod(optarg, 0); break;
+      case 'N': p->projection_width.max = strtod(optarg, 0); break;
+      case 'm': p->projection_z.min = p->projection_z.max = strtod(optarg, 0); break;
+      case 'M': p->projection_z.max = strtod(optarg, 0); break;
+      case 'p': p->algorithm = strtol(optarg, 0, 10); break;
+      case 'q': p->quadrant = true; break;
+      case 'r': p->randomize = true; break;
+      case 's': p->streams = strtol(optarg, 0, 10); break;
+      case 't': case 'T': case 'b': case 'B': case 'g': case 'G': break;  // tuning hints
+      case 'f': p->files = std::string(optarg) + "/"; break;
+      case 'F': p->projection = true; break;
+      case O_LAMBDA: p->lambda = strtod(optarg, 0); break;
+      case O_PREC:
+        if (!strcmp(optarg, "fp64")) p->precision = HOLO_FP64;
+        else if (!strcmp(optarg, "split32")) p->precision = HOLO_SPLIT32;
+        else { fprintf(stderr, "unknown precision %s\n", optarg); *exit_code = 2; return false; }
+        break;
+      case O_MC: p->mc_sub = strtol(optarg, 0, 10); break;
+      case O_SEED: p->seed = strtoull(optarg, 0, 10); break;
+      case O_MCB: p->mc_block = strtol(optarg, 0, 10); break;
+      case O_AMP: p->amplitude_only = true; break;
+      case O_REFD: p->reference_distance = strtod(optarg, 0); break;
+      case O_COMPAT: p->ref_compat = true; break;
+      case O_OUT: p->out_dir = std::string(optarg) + "/"; break;
+      case O_DEV: p->device = strtol(optarg, 0, 10); break;
+      case 'h':
+      default:
+        show_help(argv[0]);
+        *exit_code = 0;
+        return false;
+    }
+  }
+  // the reference's argument asserts (cuda/input.h:129-149), as errors
+  const double nonzero = 1e-6;
+  const char *bad = nullptr;
+  if (!(0 < p->algorithm && p->algorithm <= 3)) bad = "-p must be 1, 2 or 3";
+  else if (p->planes_obj < 1) bad = "-X must be >= 1";
+  else if (p->planes_projection > 10000) bad = "-Z must be <= 10000";
+  else if (p->n_projector == 0) bad = "-y must be > 0";
+  else if (p->planes_projection && p->n_projection == 0) bad = "-z must be > 0";
+  else if (!(p->lambda > 0.0) || !isfinite(p->lambda)) bad = "--lambda must be > 0";
+  else if (p->mc_sub < 0) bad = "--mc must be >= 1";
+  else if (p->off_z.min > 0 ? !(p->off_z.min > nonzero && p->off_z.max > nonzero)
+                            : !(-p->off_z.min > nonzero && -p->off_z.max > nonzero))
+    bad = "object z offsets must be nonzero and of one sign";
+  else if (fabs(p->off_z.min + p->projection_z.min) <= nonzero ||
+           fabs(p->off_z.min + p->projection_z.max) <= nonzero ||
+           fabs(p->off_z.max + p->projection_z.max) <= nonzero ||
+           fabs(p->off_z.max + p->projection_z.min) <= nonzero)
+    bad = "projection planes must not coincide with the projector plane";
+  if (bad) {
+    fprintf(stderr, "holo: %s\n", bad);
+    *exit_code = 2;
+    return false;
+  }
+  if (p->planes_projection == 0) p->n_projection = 1;
+  return true;
+}
+
+double now() {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+double flops(double dt, size_t n, size_t m) { return dt > 0 ? n * m * 29.0 / dt : 0.0; }  // FLOP_PER_POINT
+
+double lerp(Range<double> r, double ratio) { return (1 - ratio) * r.min + ratio * r.max; }
+
+double gerp(Range<double> r, double ratio) {
+  double a = r.min, b = r.max;
+  if (a == b) return a;
+  if (a == 0) a = 1e-12;
+  if (b == 0) b = 1e-12;
+  return pow(10, (1 - ratio) * log10(a) + ratio * log10(b));
+}
+
+// init::plane (cuda/init.h:89-158): lattice with cell-centred points; -r adds
+// the reference's cuRAND (XORWOW, seed 1235, 1236, ...) jitter.
+bool lattice(std::vector<double> &v, const holo_io::Plane &p) {
+  static unsigned int seed = 1234;
+  const size_t n = v.size() / 3;
+  for (size_t i = 0; i < n; ++i) v[3 * i + 2] = p.offset[2];
+  const size_t x = (size_t)sqrt(n * p.aspect_ratio), y = n / x;
+  const double height = p.width / p.aspect_ratio, dx = p.width / (double)x,
+               dy = height / (double)y, x_half = (p.width - dx) / 2., y_half = (height - dy) / 2.;
+  const double rel_margin = p.randomize ? 0.05 : 0.0, x_random_range = dx - 0.5 * rel_margin * dx,
+               y_random_range = dy - 0.5 * rel_margin * dy;
+  const size_t n_random = x + y;
+  std::vector<float> random(n_random);
+  curandGenerator_t gen = nullptr;
+  float *d_random = nullptr;
+  if (p.randomize) {
+    seed++;
+    if (curandCreateGenerator(&gen, CURAND_RNG_PSEUDO_XORWOW) != CURAND_STATUS_SUCCESS) return false;
+    curandSetPseudoRandomGeneratorSeed(gen, seed);
+    if (cudaMalloc((void **)&d_random, n_random * sizeof(float)) != cudaSuccess) return false;
+  }
+  for (size_t i = 0; i < x; ++i) {
+    if (p.randomize) {
+      curandGenerateUniform(gen, d_random, n_random);
+      curandGenerateUniform(gen, d_random, n_random * sizeof(float) / 32);
+      cudaMemcpy(random.data(), d_random, n_random * sizeof(float), cudaMemcpyDeviceToHost);
+    }
+    for (size_t j = 0; j < y; ++j) {
+      const size_t k = 3 * (j + i * y);
+      v[k] = i * dx - x_half + p.offset[0];
+      v[k + 1] = j * dy - y_half + p.offset[1];
+      v[k + 2] = p.offset[2];
+      if (p.randomize) {
+        v[k] += x_random_range * (random[j * 2] - 0.5);
+        v[k + 1] += y_random_range * (random[j * 2 + 1] - 0.5);
+      }
+    }
+  }
+  if (p.randomize) {
+    curandDestroyGenerator(gen);
+    cudaFree(d_random);
+  }
+  for (size_t i = x * y; i < n; ++i)
+    for (int d = 0; d < 3; ++d) v[3 * i + d] = v[d];
+  return true;
+}
+
+// init::sparse_plane with Shape::Circle (cuda/init.h:160-234)
+void circle(std::vector<double> &u, double width, const double *offset, double modulate) {
+  const size_t n = u.size() / 3;
+  for (size_t i = 0; i < n; ++i) u[3 * i + 2] = offset[2];
+  if (n == 1) {
+    u[0] = offset[0];
+    u[1] = offset[1];
+    return;
+  }
+  const double radius = width / 2.0, d_phase = kTwoPi / (double)n,
+               arbitrary_offset = 0.1125 + modulate * kTwoPi;
+  for (size_t i = 0; i < n; ++i) {
+    u[3 * i] = sin(i * d_phase + arbitrary_offset) * radius;
+    u[3 * i + 1] = cos(i * d_phase + arbitrary_offset) * radius;
+  }
+  if (offset[0] != 0 || offset[1] != 0)
+    for (size_t i = 0; i < n; ++i) {
+      u[3 * i] += offset[0];
+      u[3 * i + 1] += offset[1];
+    }
+}
+
+int lib_fail(const char *what, int rc) {
+  fprintf(stderr, "holo: %s failed (%d): %s\n", what, rc, holo_last_error_string());
+  return 3;
+}
+
+bool finite_all(const std::vector<double> &a) {
+  for (double x : a)
+    if (!isfinite(x)) return false;
+  return true;
+}
+
+struct Runner {
+  holo_handle h;
+  const Params &p;
+  // One timed pass: sources (amp, phase, pos) -> targets, normalised polar.
+  int pass(int sign, const std::vector<double> &amp, const std::vector<double> &phase,
+           const std::vector<double> &u, const std::vector<double> &v, std::vector<double> *oa,
+           std::vector<double> *op, double *dt, bool reference_wave) {
+    const size_t N = amp.size(), M = v.size() / 3;
+    oa->assign(M, 0.0);
+    op->assign(M, 0.0);
+    const double t0 = now();
+    int rc;
+    if (sign == HOLO_BACKWARDS && p.mc_sub == 0) {
+      rc = holo_project(h, p.lambda, amp.data(), phase.data(), u.data(), N, v.data(), M, nullptr,
+                        0, oa->data(), op->data(), nullptr, nullptr, p.precision,
+                        reference_wave ? 1 : 0, p.reference_distance, nullptr);
+      if (rc) return lib_fail("holo_project", rc);
+    } else {
+      std::vector<double> y(2 * M);
+      rc = p.mc_sub > 0
+               ? holo_transform_mc(h, sign, p.lambda, amp.data(), phase.data(), u.data(), N,
+                                   v.data(), M, y.data(), p.seed, p.mc_sub, p.mc_block, nullptr)
+               : holo_transform(h, sign, p.lambda, amp.data(), phase.data(), u.data(), N,
+                                v.data(), M, y.data(), p.precision, nullptr);
+      if (rc) return lib_fail("holo_transform", rc);
+      rc = holo_normalize_polar(h, y.data(), M, oa->data(), op->data(), nullptr, nullptr);
+      if (rc) return lib_fail("holo_normalize_polar", rc);
+    }
+    *dt = now() - t0;
+    if (!finite_all(*oa) || !finite_all(*op)) {
+      fprintf(stderr, "holo: non-finite output\n");
+      return 4;
+    }
+    return 0;
+  }
+};
+
+int write(const std::vector<double> &a, const std::vector<double> &ph,
+          const std::vector<double> &pos, const std::string &k1, const std::string &k2,
+          const holo_io::Plane &pl, double dt, double fl, const std::string &dir) {
+  std::string err;
+  if (!holo_io::write_arrays(a, ph, pos, k1, k2, pl, dt, fl, dir, &err)) {
+    fprintf(stderr, "holo: %s\n", err.c_str());
+    return 2;
+  }
+  return 0;
+}
+
+int file_mode(Runner &R, const Params &p) {
+  std::string err;
+  std::vector<double> xa, xp, u, v, w;
+  const std::string d = p.files;
+  if (!holo_io::read_dat(d + "x0_amp.dat", &xa, &err) ||
+      !holo_io::read_dat(d + "x0_phase.dat", &xp, &err) ||
+      !holo_io::read_dat(d + "u0.dat", &u, &err) || !holo_io::read_dat(d + "v0.dat", &v, &err)) {
+    fprintf(stderr, "holo: %s\n", err.c_str());
+    return 2;
+  }
+  if (xp.size() != xa.size() || u.size() != 3 * xa.size() || v.size() % 3) {
+    fprintf(stderr, "holo: inconsistent input sizes (x0_amp %zu, x0_phase %zu, u0 %zu, v0 %zu)\n",
+            xa.size(), xp.size(), u.size(), v.size());
+    return 2;
+  }
+  if (p.projection && !p.ref_compat) {
+    if (!holo_io::read_dat(d + "w0_0.dat", &w, &err) && !holo_io::read_dat(d + "w0.dat", &w, &err)) {
+      fprintf(stderr, "holo: %s\n", err.c_str());
+      return 2;
+    }
+  } else if (p.projection) {
+    if (!holo_io::read_dat(d + "w0.dat", &w, &err) && !holo_io::read_dat(d + "w0_0.dat", &w, &err)) {
+      fprintf(stderr, "holo: %s\n", err.c_str());
+      return 2;
+    }
+  }
+  if (w.size() % 3) {
+    fprintf(stderr, "holo: w has %zu values, not a multiple of 3\n", w.size());
+    return 2;
+  }
+  // M: v0.dat's point count, or -y when given (the reference pads with zeros or
+  // truncates to -y, cuda/transform.cu:26-41)
+  if (p.n_projector_set) v.resize(3 * p.n_projector, 0.0);
+  printf("Number of input datapoints/plane: %zu\n", xa.size());
+  const holo_io::Plane x_plane{1.0, {0.0, 0.0, 1.0}, 1.0, false};
+  const holo_io::Plane y_plane{1.0, {0.0, 0.0, 0.0}, 1.0, false};
+  const holo_io::Plane z_plane{1.0, {0.0, 0.0, 1.0}, 1.0, false};
+  (void)x_plane;
+  std::vector<double> ya, yp, za, zp;
+  double dt = 0;
+  int rc = R.pass(HOLO_BACKWARDS, xa, xp, u, v, &ya, &yp, &dt, p.amplitude_only);
+  if (rc) return rc;
+  printf("y: %zu x %zu pairs in %.6f s (%.3f TFLOPS at 29 FLOP/pair)\n", xa.size(), ya.size(), dt,
+         flops(dt, xa.size(), ya.size()) * 1e-12);
+  if ((rc = write(ya, yp, v, "y0", "v0", y_plane, dt, flops(dt, xa.size(), ya.size()), d))) return rc;
+  if (p.projection) {
+    if (p.ref_compat)
+      rc = R.pass(HOLO_FORWARDS, xa, xp, u, v, &za, &zp, &dt, false);
+    else
+      rc = R.pass(HOLO_FORWARDS, ya, yp, v, w, &za, &zp, &dt, false);
+    if (rc) return rc;
+    const size_t n_src = p.ref_compat ? xa.size() : ya.size();
+    printf("z: %zu x %zu pairs in %.6f s\n", n_src, za.size(), dt);
+    if ((rc = write(za, zp, w, "z0_0", "w0_0", z_plane, dt, flops(dt, n_src, za.size()), d)))
+      return rc;
+  }
+  return 0;
+}
+
+int generated_mode(Runner &R, const Params &p) {
+  std::vector<double> u(3 * p.n_obj), v(3 * p.n_projector), w(3 * p.n_projection);
+  std::vector<double> xa(p.n_obj, 1.0), xp(p.n_obj, 0.0);
+  // descending amplitudes: linspace(N, 1, 0) (cuda/main.cu:66-71, cuda/algebra.h linspace)
+  if (p.n_obj > 1) {
+    const double delta = (0.0 - 1.0) / (p.n_obj - 1.0);
+    for (size_t i = 0; i < p.n_obj; ++i) xa[i] = 1.0 + delta * i;
+  }
+  for (size_t i = 0; i < p.planes_obj; ++i) {
+    const double ratio = i == 0 ? 0.0 : i / ((double)p.planes_obj - 1.);
+    const double obj_off[3] = {lerp(p.off_x, ratio), lerp(p.off_y, ratio), gerp(p.off_z, ratio)};
+    holo_io::Plane x_plane{lerp(p.obj_width, ratio), {obj_off[0], obj_off[1], obj_off[2]}, 1.0,
+                           false};
+    circle(u, x_plane.width, obj_off, i / (double)p.planes_obj);
+    holo_io::Plane y_plane{lerp(p.projector_width, ratio), {0, 0, 0}, p.aspect_projector,
+                           p.randomize};
+    if (!lattice(v, y_plane)) return lib_fail("cuRAND", -2);
+    const std::string xs = std::to_string(i);
+    int rc;
+    if ((rc = write(xa, xp, u, "x" + xs, "u" + xs, x_plane, 0.0, 0.0, p.out_dir))) return rc;
+    std::vector<double> ya, yp;
+    double dt = 0;
+    if ((rc = R.pass(HOLO_BACKWARDS, xa, xp, u, v, &ya, &yp, &dt, p.amplitude_only))) return rc;
+    if ((rc = write(ya, yp, v, "y" + xs, "v" + xs, y_plane, dt, flops(dt, xa.size(), ya.size()),
+                    p.out_dir)))
+      return rc;
+    for (size_t j = 0; j < p.planes_projection; ++j) {
+      const double r2 = j == 0 ? 0.0 : j / ((double)p.planes_projection - 1.);
+      const double width = gerp(p.projection_width, r2), height = width / p.aspect_projection;
+      const double po[3] = {p.quadrant ? width / 2. : 0., p.quadrant ? height / 2. : 0.,
+                            lerp(p.projection_z, r2)};
+      holo_io::Plane z_plane{width,
+                             {obj_off[0] + po[0], obj_off[1] + po[1], obj_off[2] + po[2]},
+                             p.aspect_projection,
+                             p.randomize};
+      if (!lattice(w, z_plane)) return lib_fail("cuRAND", -2);
+      std::vector<double> za, zp;
+      if ((rc = R.pass(HOLO_FORWARDS, ya, yp, v, w, &za, &zp, &dt, false))) return rc;
+      const std::string zs = xs + "_" + std::to_string(j);
+      if ((rc = write(za, zp, w, "z" + zs, "w" + zs, z_plane, dt,
+                      flops(dt, ya.size(), za.size()), p.out_dir)))
+        return rc;
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  Params p;
+  int code = 0;
+  if (!parse(argc, argv, &p, &code)) return code;
+  holo_handle h = nullptr;
+  int rc = holo_create(p.device, &h);
+  if (rc) return lib_fail("holo_create", rc);
+  Runner R{h, p};
+  rc = p.files.empty() ? generated_mode(R, p) : file_mode(R, p);
+  holo_destroy(h);
+  if (rc == 0) printf("done\n");
+  return rc;
+}

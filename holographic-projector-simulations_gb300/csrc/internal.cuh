@@ -1,0 +1,217 @@
+// internal.cuh -- shared declarations of the GB300 Huygens superposition library.
+//
+// Layout in HBM (per point set, after planning):
+//   pos     FP64 xyz, absolute positions in tile order, padded with zeros to a
+//           multiple of the source tile (bulk-copy granularity)
+//   ap      FP64 (phase, amp) pairs of the sources in tile order (per execute)
+//   tiles   per tile of `tile` consecutive points: FP64 centre xyz + half-extent xyz
+//   order   int32, tile-order position -> original index
+//   partial FP64 complex [splits][M] cross-CTA partial sums (scratch)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "holo.h"
+
+namespace holo {
+
+// ---- constants -----------------------------------------------------------
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+// Two-constant Cody-Waite split of 2 pi for FP64 range reduction:
+// kTwoPiHi = fl64(2 pi), kTwoPiLo = 2 pi - kTwoPiHi.
+constexpr double kTwoPiHi = 6.283185307179586232;
+constexpr double kTwoPiLo = 2.4492935982947064e-16;
+constexpr double kInvTwoPi = 0.15915494309189533577;
+
+constexpr int kHilbertGrid = 64;                 // cells per axis of the tiling sort
+constexpr int kCells = kHilbertGrid * kHilbertGrid;
+constexpr int kSortBlock = 4096;                 // points per block of the counting sort
+constexpr long long kWaitCycles = 4000000000LL;  // bounded device wait (~2 s at 2 GHz)
+
+// device error word values (written by kernels, read by holo_device_status)
+constexpr int kDevErrTimeout = 1;
+
+// ---- error reporting ---------------------------------------------------------
+void set_error(const char *fmt, ...);
+int fail(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define HOLO_CUDA(expr)                                                  \
+  do {                                                                   \
+    cudaError_t _e = (expr);                                             \
+    if (_e != cudaSuccess) return ::holo::cuda_fail(_e, #expr, __FILE__, __LINE__); \
+  } while (0)
+
+#define HOLO_TRY(expr)            \
+  do {                            \
+    int _rc = (expr);             \
+    if (_rc != HOLO_OK) return _rc; \
+  } while (0)
+
+// ---- kernel variants -----------------------------------------------------------
+struct Variant {
+  int threads;  // threads per CTA
+  int r;        // targets per thread (register blocking)
+  int cs;       // sources per tile (one bulk copy per tile)
+  int tt() const { return threads * r; }
+};
+
+int split_variant_count();
+Variant split_variant(int i);
+int fp64_variant_count();
+Variant fp64_variant(int i);
+
+// ---- device-side problem descriptor (one plan execute) ------------------------
+struct SplitProblem {
+  const double *pos_s;     // sources, tile order, absolute xyz (3 * Ns_pad)
+  const double2 *ap_s;     // sources, tile order, (phase, amp)   (Ns_pad)
+  const double *tiles_s;   // source tiles of `cs` points: centre xyz, half xyz
+  const double *pos_t;     // targets, tile order, absolute xyz (3 * M)
+  const double *tiles_t;   // target tiles of `tt` points
+  const int32_t *order_t;  // target tile order -> original index
+  double2 *partial;        // [splits][M] (tile order) when splits > 1
+  double2 *y;              // output, original target order, when splits == 1
+  int N, M;
+  int n_stiles, n_ttiles, splits;
+  int sign;
+  double sk;               // sign * k
+  // Monte Carlo
+  uint32_t seed_lo, seed_hi;
+  int sub;                 // sources per stratum
+};
+
+struct Fp64Problem {
+  const double *pos_s;     // original order, absolute xyz (3 * Ns_pad)
+  const double2 *ap_s;     // (phase, amp) (Ns_pad)
+  const double *pos_t;     // original order xyz (3 * M)
+  double2 *partial;        // [splits][M]
+  double2 *y;              // output when splits == 1
+  int N, M;
+  int n_stiles, n_ttiles, splits;
+  int sign;
+  double k;
+};
+
+// batched work item: problem index, target tile, [s_begin, s_end) source tiles, split slot
+struct WorkItem {
+  int problem, ttile, s_begin, s_end, split, pad0, pad1, pad2;
+};
+
+// ---- launchers (defined in the .cu files) --------------------------------------
+// probe.cu: count of kernels this library launched (reported by the benchmark)
+void note_launches(int n);
+
+// tiler.cu
+int launch_bbox(const double *pos, int n, double *bbox6, double *scratch, int scratch_blocks,
+                cudaStream_t s);
+int sort_points(const double *pos, int n, const double *bbox6, int32_t *order, uint16_t *keys,
+                uint32_t *hist, uint32_t *scan_tmp, cudaStream_t s);
+size_t sort_hist_entries(int n);
+int launch_gather_pos(const double *pos, const int32_t *order, int n, int n_pad, double *out,
+                      cudaStream_t s);
+int launch_tile_bbox(const double *pos_sorted, int n, int tile, double *tiles, cudaStream_t s);
+int launch_gather_ap(const double *amp, const double *phase, const int32_t *order, int n,
+                     int n_pad, double2 *out, cudaStream_t s);
+int launch_pack_ap(const double *amp, const double *phase, int n, int n_pad, double2 *out,
+                   cudaStream_t s);
+int launch_pack_pos(const double *pos, int n, int n_pad, double *out, cudaStream_t s);
+int launch_iota(int32_t *order, int n, cudaStream_t s);
+
+// kernel_split.cu
+int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
+                 int *err, cudaStream_t s);
+int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,
+                         int *queue, int variant, int grid, int *err, cudaStream_t s);
+int split_occupancy(int variant, bool mc, int *ctas_per_sm);
+int split_smem_bytes(int variant);
+
+// kernel_fp64.cu
+int launch_fp64(const Fp64Problem &p, int variant, int grid, bool const_phase, int *err,
+                cudaStream_t s);
+int fp64_occupancy(int variant, int *ctas_per_sm);
+
+// epilogue.cu
+int launch_reduce(const double2 *partial, int splits, int M, const int32_t *order,
+                  double2 *y, cudaStream_t s);
+int launch_reduce_batched(const SplitProblem *probs_dev, const int *prob_offsets, int n_probs,
+                          int total_targets, cudaStream_t s);
+int launch_max_abs(const double2 *y, int M, double *partials, int n_partials, double *max_out,
+                   cudaStream_t s);
+int launch_normalize_polar(const double2 *y, int M, const double *max_abs, double *amp,
+                           double *phase, cudaStream_t s);
+int launch_complex_to_polar(const double2 *g, int M, double *amp, double *phase,
+                            cudaStream_t s);
+int launch_adjoint_epilogue(const double2 *h, const double *amp, const double *phase, int N,
+                            double *grad_amp, double *grad_phase, cudaStream_t s);
+int launch_reference_wave(double2 *y, const double2 *y_ref, int M, const double *max_y,
+                          const double *max_ref, double *amp_out, double *phase_out,
+                          cudaStream_t s);
+
+}  // namespace holo
+
+// ---- handle, plan, batch -----------------------------------------------------------
+struct holo_handle_s {
+  int device = 0;
+  int sm_count = 0;
+  cudaMemPool_t pool = nullptr;
+  int *dev_err = nullptr;  // device error word
+  std::mutex mu;
+  // CUDA-event pairs around each pair-evaluation kernel while profiling is on
+  bool profiling = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof;
+  // variant table per precision x size bucket (-1 = built-in choice)
+  int variant_table[2][8] = {{-1, -1, -1, -1, -1, -1, -1, -1}, {-1, -1, -1, -1, -1, -1, -1, -1}};
+};
+
+struct holo_plan_s {
+  holo_handle h = nullptr;
+  int precision = HOLO_SPLIT32;
+  int N = 0, M = 0;
+  int n_pad = 0;                 // padded source count
+  int variant = 0;
+  int splits = 1;
+  int grid = 0;
+  int n_stiles = 0, n_ttiles = 0;
+  cudaStream_t last_stream = nullptr;
+  // device buffers
+  double *pos_s = nullptr;       // 3 * n_pad
+  double *pos_t = nullptr;       // 3 * M
+  double *tiles_s = nullptr;     // 6 * n_stiles
+  double *tiles_t = nullptr;     // 6 * n_ttiles
+  int32_t *order_s = nullptr;    // N (split only)
+  int32_t *order_t = nullptr;    // M (split only)
+  double *u_orig = nullptr;      // original-order positions (for the adjoint)
+  double *v_orig = nullptr;
+  std::vector<void *> owned;     // everything allocated for the plan
+  // adjoint: the transposed plan (targets become sources), built on first use
+  holo_plan_s *transposed = nullptr;
+};
+
+struct holo_batch_s {
+  holo_handle h = nullptr;
+  std::vector<holo_plan_s *> plans;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<void *> owned;
+  long long total_pairs = 0;
+};
+
+namespace holo {
+// abi.cu helpers shared with the autotuner
+void *pool_alloc(holo_handle h, size_t bytes, cudaStream_t s);
+void pool_free(void *p, cudaStream_t s);
+int size_bucket(size_t N, size_t M);
+int plan_create_impl(holo_handle h, const double *u_dev, size_t N, const double *v_dev,
+                     size_t M, int precision, int forced_variant, cudaStream_t s,
+                     holo_plan_s **out);
+int plan_execute_impl(holo_plan_s *p, int sign, double lambda, const double *amp_dev,
+                      const double *phase_dev, double2 *y_dev, int flags, cudaStream_t s);
+void plan_release(holo_plan_s *p, cudaStream_t s);
+// probe.cu: bracket a pair-evaluation kernel with events while profiling
+int profile_mark(holo_handle h, cudaStream_t s, bool begin);
+}  // namespace holo

@@ -1,0 +1,465 @@
+// kernel_split.cu -- split-precision Huygens superposition (HOLO_SPLIT32).
+//
+// Reference hot path: superposition::per_block + phasor_displacement
+// (cuda/superposition.cu:35-51, 59-154) in FP64.  Here each CTA owns a tile of
+// TT = THREADS * R targets (R per thread, in registers) and walks source tiles
+// of CS points that a TMA bulk copy stages in shared memory (double-buffered,
+// mbarrier-tracked).  For every (target tile, source tile) pair a frame is
+// built in FP64 from the two tile centres T0, S0:
+//   D = T0 - S0, r0 = |D|, e = D / r0, (e1, e2) an orthonormal basis of e-perp.
+// With t' = t - T0, s' = s - S0 and d = t' - s':
+//   r = |D + d| = q + rho,   q = r0 + e.d,   c = |d_perp|^2,
+//   rho = c / (q + r) = (c / 2r) (1 + c / (4 r^2) + O(c^2 / r^4)),
+//   s k r = [phi-independent] s k (r0 + e.t')  - s k e.s'  + s k rho.
+// The two linear terms are separable and large (k |t'| ~ 1e3 rad): they are
+// evaluated in FP64 once per target (B) and once per source (A) per tile pair
+// and reduced mod 2 pi (two-constant Cody-Waite).  Per pair only the small
+// curvature term s k rho (|rho| / r0 ~ 1e-6) and the amplitude 1/r are formed
+// in FP32; their sensitivity to FP32 rounding of d is suppressed by |d| / r0.
+// Per pair: 14 FP32 ops + 3 MUFU ops (rsqrt, sin, cos).  Sums run in FP32
+// over one source tile (CS terms), are rotated by e^{iB} and carried in FP64.
+#include "internal.cuh"
+#include "ptx.cuh"
+
+namespace holo {
+namespace {
+
+struct __align__(16) Frame {
+  double e[3];
+  double r0;
+  double b0;     // s k r0 reduced mod 2 pi
+  double t0[3];  // target tile centre
+  double s0[3];  // source tile centre
+  float ef[3], e1[3], e2[3];
+  float r0f;
+};
+
+// Philox4x32-10 (Salmon et al., SC'11); same rounds as the oracle.
+__device__ __forceinline__ uint32_t philox_first(uint32_t c0, uint32_t c1, uint32_t k0,
+                                                 uint32_t k1) {
+  uint32_t c2 = 0, c3 = 0;
+#pragma unroll
+  for (int round = 0; round < 10; ++round) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c0;
+}
+
+__device__ __forceinline__ void build_frame(Frame *fr, const double *t0, const double *s0,
+                                            double sk) {
+  double D[3], r2 = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    fr->t0[d] = t0[d];
+    fr->s0[d] = s0[d];
+    D[d] = t0[d] - s0[d];
+    r2 = fma(D[d], D[d], r2);
+  }
+  const double r0 = sqrt(r2);
+  const double inv = r0 > 0.0 ? 1.0 / r0 : 0.0;
+  double e[3] = {D[0] * inv, D[1] * inv, D[2] * inv};
+  if (r0 == 0.0) { e[0] = 0.0; e[1] = 0.0; e[2] = 1.0; }
+  // e1: the coordinate axis least aligned with e, made orthogonal to e
+  const double ax = fabs(e[0]), ay = fabs(e[1]), az = fabs(e[2]);
+  double a[3] = {0.0, 0.0, 0.0};
+  if (ax <= ay && ax <= az) a[0] = 1.0; else if (ay <= az) a[1] = 1.0; else a[2] = 1.0;
+  const double ae = a[0] * e[0] + a[1] * e[1] + a[2] * e[2];
+  double e1[3] = {a[0] - ae * e[0], a[1] - ae * e[1], a[2] - ae * e[2]};
+  const double n1 = rsqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+  for (int d = 0; d < 3; ++d) e1[d] *= n1;
+  const double e2[3] = {e[1] * e1[2] - e[2] * e1[1], e[2] * e1[0] - e[0] * e1[2],
+                        e[0] * e1[1] - e[1] * e1[0]};
+  for (int d = 0; d < 3; ++d) {
+    fr->e[d] = e[d];
+    fr->ef[d] = (float)e[d];
+    fr->e1[d] = (float)e1[d];
+    fr->e2[d] = (float)e2[d];
+  }
+  fr->r0 = r0;
+  fr->r0f = (float)r0;
+  fr->b0 = reduce_two_pi(sk * r0);
+}
+
+template <int THREADS, int R, int CS>
+struct SplitSmem {
+  static constexpr size_t raw_pos = 0;                                   // double [2][CS*3]
+  static constexpr size_t raw_ap = raw_pos + 2 * CS * 3 * sizeof(double);  // double2 [2][CS]
+  static constexpr size_t rec = raw_ap + 2 * CS * sizeof(double2);        // float4 [CS]
+  static constexpr size_t amp = rec + CS * sizeof(float4);                // float [CS]
+  static constexpr size_t acc = (amp + CS * sizeof(float) + 15) / 16 * 16;  // double2 [R][THREADS]
+  static constexpr size_t bphase = acc + R * THREADS * sizeof(double2);      // float [R][THREADS]
+  static constexpr size_t frame = (bphase + R * THREADS * sizeof(float) + 15) / 16 * 16;
+  static constexpr size_t bar = frame + sizeof(Frame);                    // uint64 [2]
+  static constexpr size_t bytes = bar + 2 * sizeof(uint64_t);
+};
+
+// Process one work item: target tile `tt`, source tiles [sb, se), writing into
+// partial slot `split` (or the final output when the problem has one split).
+template <int THREADS, int R, int CS, bool CONST, bool MC>
+__device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int split, int sb,
+                                             int se, unsigned char *smem, uint32_t &par0,
+                                             uint32_t &par1, int *err) {
+  using L = SplitSmem<THREADS, R, CS>;
+  constexpr int TT = THREADS * R;
+  double *raw_pos = reinterpret_cast<double *>(smem + L::raw_pos);
+  double2 *raw_ap = reinterpret_cast<double2 *>(smem + L::raw_ap);
+  float4 *rec = reinterpret_cast<float4 *>(smem + L::rec);
+  float *ramp = reinterpret_cast<float *>(smem + L::amp);
+  Frame *fr = reinterpret_cast<Frame *>(smem + L::frame);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::bar);
+  // FP64 carries and the per-target phase B live in shared memory (index
+  // [r][tid]) so that the pair loop keeps only 5 R registers per thread.
+  double2 *acc = reinterpret_cast<double2 *>(smem + L::acc);
+  float *bph = reinterpret_cast<float *>(smem + L::bphase);
+  const int tid = threadIdx.x;
+  const double sk = P.sk;
+  const float kap2 = (float)(0.5 * sk);    // s k / 2
+  const float kap8 = (float)(0.125 * sk);  // s k / 8
+  const int n_strata = MC ? (P.N + P.sub - 1) / P.sub : 0;
+
+  auto issue = [&](int j, int buf) {
+    // tile j of CS sources: CS*24 B of positions + CS*16 B of (phase, amp)
+    ptx::mbar_arrive_expect_tx(&bar[buf], CS * (3 * sizeof(double) + sizeof(double2)));
+    ptx::bulk_g2s(raw_pos + buf * CS * 3, P.pos_s + (size_t)j * CS * 3,
+                  CS * 3 * sizeof(double), &bar[buf]);
+    ptx::bulk_g2s(raw_ap + buf * CS, P.ap_s + (size_t)j * CS, CS * sizeof(double2),
+                  &bar[buf]);
+  };
+
+  if (!MC && tid == 0 && sb < se) issue(sb, 0);
+
+#pragma unroll
+  for (int r = 0; r < R; ++r) acc[r * THREADS + tid] = make_double2(0.0, 0.0);
+
+  for (int j = sb; j < se; ++j) {
+    const int buf = (j - sb) & 1;
+    if (!MC && tid == 0 && j + 1 < se) issue(j + 1, buf ^ 1);
+    if (tid == 0) {
+      const double *tc = P.tiles_t + 6 * (size_t)tt;
+      double sc[3];
+      if (!MC) {
+        for (int d = 0; d < 3; ++d) sc[d] = P.tiles_s[6 * (size_t)j + d];
+      } else {
+        // union of the source tiles that hold this chunk's strata
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        const int t_first = j * P.sub;
+        const int t_last = min(P.n_stiles, (j + 1) * P.sub);
+        for (int t = t_first; t < t_last; ++t)
+          for (int d = 0; d < 3; ++d) {
+            const double c = P.tiles_s[6 * (size_t)t + d], h = P.tiles_s[6 * (size_t)t + 3 + d];
+            lo[d] = fmin(lo[d], c - h);
+            hi[d] = fmax(hi[d], c + h);
+          }
+        for (int d = 0; d < 3; ++d) sc[d] = 0.5 * (lo[d] + hi[d]);
+      }
+      build_frame(fr, tc, sc, sk);
+    }
+    if (!MC) {
+      const uint32_t par = buf ? par1 : par0;
+      const bool ok = ptx::mbar_wait_bounded(&bar[buf], par, kWaitCycles);
+      if (buf) par1 ^= 1u; else par0 ^= 1u;
+      if (!__syncthreads_and(ok)) {
+        if (tid == 0) atomicExch(err, kDevErrTimeout);
+        return false;
+      }
+    } else {
+      __syncthreads();
+    }
+
+    // ---- phase A: per-source records of this tile pair ----
+    const double e0 = fr->e[0], e1_ = fr->e[1], e2_ = fr->e[2];
+    const float f1x = fr->e1[0], f1y = fr->e1[1], f1z = fr->e1[2];
+    const float f2x = fr->e2[0], f2y = fr->e2[1], f2z = fr->e2[2];
+    for (int i = tid; i < CS; i += THREADS) {
+      bool valid;
+      double sx, sy, sz, ph, am;
+      if (!MC) {
+        valid = j * CS + i < P.N;
+        const double *sp = raw_pos + buf * CS * 3 + 3 * i;
+        const double2 a2 = raw_ap[buf * CS + i];
+        sx = sp[0]; sy = sp[1]; sz = sp[2];
+        ph = a2.x; am = a2.y;
+      } else {
+        const int st = j * CS + i;
+        valid = st < n_strata;
+        sx = sy = sz = ph = am = 0.0;
+        if (valid) {
+          const int start = st * P.sub;
+          const int size = min(P.sub, P.N - start);
+          const uint32_t rnd = philox_first((uint32_t)st, (uint32_t)tt, P.seed_lo, P.seed_hi);
+          const int sidx = start + (int)(rnd % (uint32_t)size);
+          const double *sp = P.pos_s + 3 * (size_t)sidx;
+          const double2 a2 = P.ap_s[sidx];
+          sx = sp[0]; sy = sp[1]; sz = sp[2];
+          ph = a2.x;
+          am = a2.y * (double)size;
+          if (CONST) am = (double)size;
+        }
+      }
+      float4 q;
+      float a;
+      if (valid) {
+        const double dx = sx - fr->s0[0], dy = sy - fr->s0[1], dz = sz - fr->s0[2];
+        const double ps = fma(e0, dx, fma(e1_, dy, e2_ * dz));
+        const double A = CONST ? 0.0 : reduce_two_pi(fma(-sk, ps, ph));
+        const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+        q.x = fmaf(f1x, fx, fmaf(f1y, fy, f1z * fz));
+        q.y = fmaf(f2x, fx, fmaf(f2y, fy, f2z * fz));
+        q.z = (float)ps;
+        q.w = (float)A;
+        a = CONST ? (MC ? (float)am : 1.0f) : (float)am;
+      } else {
+        q = make_float4(0.f, 0.f, -1e18f, 0.f);  // r ~ 1e18: contributes 0
+        a = 0.f;
+      }
+      rec[i] = q;
+      ramp[i] = a;
+    }
+
+    // ---- per-thread target frame ----
+    float Tx[R], Ty[R], Qt[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int ti = tt * TT + tid + r * THREADS;
+      double tx = 0.0, ty = 0.0, tz = 0.0;
+      if (ti < P.M) {
+        const double *tp = P.pos_t + 3 * (size_t)ti;
+        tx = tp[0] - fr->t0[0];
+        ty = tp[1] - fr->t0[1];
+        tz = tp[2] - fr->t0[2];
+      }
+      const double pt = fma(e0, tx, fma(e1_, ty, e2_ * tz));
+      const double B = reduce_two_pi(fma(sk, pt, fr->b0));
+      const float fx = (float)tx, fy = (float)ty, fz = (float)tz;
+      Tx[r] = fmaf(f1x, fx, fmaf(f1y, fy, f1z * fz));
+      Ty[r] = fmaf(f2x, fx, fmaf(f2y, fy, f2z * fz));
+      Qt[r] = (float)(fr->r0 + pt);
+      bph[r * THREADS + tid] = (float)B;
+    }
+    __syncthreads();
+
+    // ---- pair loop: CS sources x R targets ----
+    float re[R], im[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      re[r] = 0.f;
+      im[r] = 0.f;
+    }
+#pragma unroll 2
+    for (int s = 0; s < CS; ++s) {
+      const float4 q = rec[s];
+      const float a = ramp[s];
+      if (CONST) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) re[r] += a;
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const float dx = Tx[r] - q.x;
+          const float dy = Ty[r] - q.y;
+          const float c = fmaf(dy, dy, dx * dx);
+          const float qq = Qt[r] - q.z;
+          const float r2 = fmaf(qq, qq, c);
+          const float ir = ptx::rsqrt_approx(r2);
+          const float h = c * ir;
+          const float g = h * ir;
+          const float th = fmaf(h, fmaf(g, kap8, kap2), q.w);
+          const float w = a * ir;
+          re[r] = fmaf(w, ptx::cos_approx(th), re[r]);
+          im[r] = fmaf(w, ptx::sin_approx(th), im[r]);
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      double2 a = acc[r * THREADS + tid];
+      if (CONST) {
+        a.x += (double)re[r];
+        a.y += (double)im[r];
+      } else {
+        float sb, cb;
+        __sincosf(bph[r * THREADS + tid], &sb, &cb);
+        a.x += (double)fmaf(re[r], cb, -im[r] * sb);
+        a.y += (double)fmaf(re[r], sb, im[r] * cb);
+      }
+      acc[r * THREADS + tid] = a;
+    }
+    __syncthreads();  // rec, ramp and the frame are rewritten next tile
+  }
+
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int ti = tt * TT + tid + r * THREADS;
+    if (ti < P.M) {
+      const double2 v = acc[r * THREADS + tid];
+      if (P.splits == 1)
+        P.y[P.order_t[ti]] = v;
+      else
+        P.partial[(size_t)split * P.M + ti] = v;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void split_range(int n, int splits, int s, int *b, int *e) {
+  *b = (int)(((long long)n * s) / splits);
+  *e = (int)(((long long)n * (s + 1)) / splits);
+}
+
+template <int THREADS, int R, int CS, bool CONST, bool MC>
+__global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
+    k_split(const SplitProblem P, int n_items, int *err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  using L = SplitSmem<THREADS, R, CS>;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::bar);
+  if (threadIdx.x == 0) {
+    ptx::mbar_init(&bar[0], 1);
+    ptx::mbar_init(&bar[1], 1);
+    ptx::fence_barrier_init();
+  }
+  __syncthreads();
+  uint32_t par0 = 0, par1 = 0;
+  const int n_src = MC ? ((P.N + P.sub - 1) / P.sub + CS - 1) / CS : P.n_stiles;
+  for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const int tt = item / P.splits;
+    const int split = item % P.splits;
+    int sb, se;
+    split_range(n_src, P.splits, split, &sb, &se);
+    if (!process_item<THREADS, R, CS, CONST, MC>(P, tt, split, sb, se, smem, par0, par1, err))
+      return;
+  }
+}
+
+template <int THREADS, int R, int CS>
+__global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
+    k_split_batched(const SplitProblem *__restrict__ probs, const WorkItem *__restrict__ items,
+                    int n_items, int *queue, int *err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  using L = SplitSmem<THREADS, R, CS>;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::bar);
+  __shared__ int s_item;
+  if (threadIdx.x == 0) {
+    ptx::mbar_init(&bar[0], 1);
+    ptx::mbar_init(&bar[1], 1);
+    ptx::fence_barrier_init();
+  }
+  uint32_t par0 = 0, par1 = 0;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n_items) break;
+    const WorkItem w = items[it];
+    const SplitProblem P = probs[w.problem];
+    if (!process_item<THREADS, R, CS, false, false>(P, w.ttile, w.split, w.s_begin, w.s_end,
+                                                    smem, par0, par1, err))
+      return;
+  }
+}
+
+// ---- variant table ------------------------------------------------------------
+constexpr Variant kVariants[] = {
+    {256, 8, 512},  // 0: TT 2048
+    {128, 8, 512},  // 1: TT 1024
+    {256, 4, 512},  // 2: TT 1024
+    {128, 4, 256},  // 3: TT 512
+    {128, 2, 256},  // 4: TT 256 (Monte Carlo blocks of 256 targets)
+    {256, 8, 1024}, // 5: TT 2048, long source tiles
+};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+template <int THREADS, int R, int CS, bool CONST, bool MC>
+int launch_one(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
+  using L = SplitSmem<THREADS, R, CS>;
+  auto kern = k_split<THREADS, R, CS, CONST, MC>;
+  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)L::bytes));
+  const int n_items = p.n_ttiles * p.splits;
+  if (n_items <= 0) return HOLO_OK;
+  kern<<<grid, THREADS, L::bytes, s>>>(p, n_items, err); note_launches(1);
+  HOLO_CUDA(cudaGetLastError());
+  return HOLO_OK;
+}
+
+template <int THREADS, int R, int CS>
+int launch_variant(const SplitProblem &p, int grid, bool cst, bool mc, int *err,
+                   cudaStream_t s) {
+  if (cst && mc) return launch_one<THREADS, R, CS, true, true>(p, grid, err, s);
+  if (cst) return launch_one<THREADS, R, CS, true, false>(p, grid, err, s);
+  if (mc) return launch_one<THREADS, R, CS, false, true>(p, grid, err, s);
+  return launch_one<THREADS, R, CS, false, false>(p, grid, err, s);
+}
+
+template <int THREADS, int R, int CS>
+int batched_variant(const SplitProblem *probs, const WorkItem *items, int n_items, int *queue,
+                    int grid, int *err, cudaStream_t s) {
+  using L = SplitSmem<THREADS, R, CS>;
+  auto kern = k_split_batched<THREADS, R, CS>;
+  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)L::bytes));
+  kern<<<grid, THREADS, L::bytes, s>>>(probs, items, n_items, queue, err); note_launches(1);
+  HOLO_CUDA(cudaGetLastError());
+  return HOLO_OK;
+}
+
+template <int THREADS, int R, int CS>
+int occupancy_variant(bool mc, int *out) {
+  using L = SplitSmem<THREADS, R, CS>;
+  auto kern = mc ? k_split<THREADS, R, CS, false, true> : k_split<THREADS, R, CS, false, false>;
+  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)L::bytes));
+  HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, THREADS, L::bytes));
+  return HOLO_OK;
+}
+
+}  // namespace
+
+int split_variant_count() { return kNumVariants; }
+Variant split_variant(int i) { return kVariants[i]; }
+
+#define HOLO_SPLIT_DISPATCH(V, CALL)                      \
+  switch (V) {                                            \
+    case 0: return CALL(256, 8, 512);                     \
+    case 1: return CALL(128, 8, 512);                     \
+    case 2: return CALL(256, 4, 512);                     \
+    case 3: return CALL(128, 4, 256);                     \
+    case 4: return CALL(128, 2, 256);                     \
+    case 5: return CALL(256, 8, 1024);                    \
+    default: return fail(HOLO_ERR_INVALID, "unknown split variant %d", V); \
+  }
+
+int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
+                 int *err, cudaStream_t s) {
+#define CALL(T, R, C) launch_variant<T, R, C>(p, grid, const_phase, mc, err, s)
+  HOLO_SPLIT_DISPATCH(variant, CALL)
+#undef CALL
+}
+
+int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,
+                         int *queue, int variant, int grid, int *err, cudaStream_t s) {
+#define CALL(T, R, C) batched_variant<T, R, C>(probs_dev, items, n_items, queue, grid, err, s)
+  HOLO_SPLIT_DISPATCH(variant, CALL)
+#undef CALL
+}
+
+int split_occupancy(int variant, bool mc, int *ctas_per_sm) {
+#define CALL(T, R, C) occupancy_variant<T, R, C>(mc, ctas_per_sm)
+  HOLO_SPLIT_DISPATCH(variant, CALL)
+#undef CALL
+}
+
+int split_smem_bytes(int variant) {
+#define CALL(T, R, C) (int)SplitSmem<T, R, C>::bytes
+  HOLO_SPLIT_DISPATCH(variant, CALL)
+#undef CALL
+}
+
+}  // namespace holo

@@ -1,0 +1,187 @@
+"""GPU parity: every precision mode against the CPU FP64 oracle, through the C ABI.
+
+Tolerances (relative L2 over the field):
+  HOLO_FP64    1e-12  (same rounding sequence per term as the oracle)
+  HOLO_SPLIT32 1e-5   (the precision target of the split-precision path)
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, LAM, config1, config2, grid, max_phase_err, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-12, "split32": 1e-5}
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split32"])
+def test_golden_small_transform(holo, orc, prec):
+    g = np.load(os.path.join(GOLDEN, "transform_small.npz"))
+    lam = float(g["lam"])
+    y = holo.transform(g["amp"], g["phase"], g["u"], g["v"], -1, lam, precision=prec)
+    ref = orc.transform(g["amp"], g["phase"], g["u"], g["v"], -1, lam)
+    assert rel_l2(y, ref) < TOL[prec]
+    # against the reference's own terms (pow vs sqrt distance: <= 1e-10)
+    assert rel_l2(y, g["y"]) < max(TOL[prec], 1e-10)
+    z = holo.transform(g["y_amp"], g["y_phase"], g["v"], g["w"], +1, lam, precision=prec)
+    assert rel_l2(z, g["z"]) < max(TOL[prec], 1e-10)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split32"])
+def test_config1_chain(holo, orc, prec):
+    """Config 1: 4096 sources -> 65,536 projector pixels -> 4096 projection points."""
+    amp, phase, u, v, w = config1()
+    y = holo.transform(amp, phase, u, v, -1, LAM, precision=prec)
+    y_ref = orc.transform(amp, phase, u, v, -1, LAM)
+    assert rel_l2(y, y_ref) < TOL[prec]
+    yn, _ = orc.normalize_amp(y_ref)
+    ya, yp = orc.to_polar(yn)
+    z = holo.transform(ya, yp, v, w, +1, LAM, precision=prec)
+    z_ref = orc.transform(ya, yp, v, w, +1, LAM)
+    assert rel_l2(z, z_ref) < TOL[prec]
+    if prec == "split32":
+        assert max_phase_err(y, y_ref) < 1e-3
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split32"])
+def test_project_chain_matches_oracle(holo, orc, prec):
+    """holo_project: normalised polar y and z (cuda/main.cu:186, 213-216 semantics)."""
+    amp, phase, u, v, w = config1(seed=5)
+    u, v, w = u[:1024], v[:16384], w[:2048]
+    amp, phase = amp[:1024], phase[:1024]
+    ya, yp, za, zp = holo.project(amp, phase, u, v, w, LAM, precision=prec)
+    y = orc.transform(amp, phase, u, v, -1, LAM)
+    yn, _ = orc.normalize_amp(y)
+    ra, rp = orc.to_polar(yn)
+    assert rel_l2(ya * np.exp(1j * yp), ra * np.exp(1j * rp)) < TOL[prec] * 10
+    z = orc.transform(ra, rp, v, w, +1, LAM)
+    zn, _ = orc.normalize_amp(z)
+    qa, qp = orc.to_polar(zn)
+    assert rel_l2(za * np.exp(1j * zp), qa * np.exp(1j * qp)) < max(TOL[prec] * 10, 1e-10)
+    assert np.max(ya) == pytest.approx(1.0) and np.max(za) == pytest.approx(1.0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split32"])
+@pytest.mark.parametrize("n,m", [(1, 1), (1, 3000), (7, 5), (513, 2049), (3000, 1),
+                                 (1025, 777)])
+def test_ragged_sizes(holo, orc, prec, n, m):
+    rng = np.random.default_rng(n * 31 + m)
+    u = np.column_stack([rng.uniform(-1e-3, 1e-3, (n, 2)), np.full(n, 0.3)])
+    v = np.column_stack([rng.uniform(-2e-3, 2e-3, (m, 2)), np.zeros(m)])
+    amp, phase = rng.uniform(0, 1, n), rng.uniform(0, 2 * np.pi, n)
+    for sign in (-1, 1):
+        y = holo.transform(amp, phase, u, v, sign, LAM, precision=prec)
+        assert rel_l2(y, orc.transform(amp, phase, u, v, sign, LAM)) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split32"])
+def test_tilted_and_3d_geometry(holo, orc, prec):
+    """Non-parallel planes and a 3-D cloud (the frame basis is built per tile pair)."""
+    rng = np.random.default_rng(11)
+    n, m = 2000, 5000
+    s = rng.uniform(-1.5e-3, 1.5e-3, (n, 2))
+    u = np.column_stack([s[:, 0], s[:, 1], 0.25 + 0.3 * s[:, 0]])  # tilted source plane
+    v = np.column_stack([rng.uniform(-2e-3, 2e-3, (m, 2)), rng.uniform(-5e-4, 5e-4, m)])
+    amp, phase = rng.uniform(0, 1, n), rng.uniform(0, 2 * np.pi, n)
+    y = holo.transform(amp, phase, u, v, -1, LAM, precision=prec)
+    assert rel_l2(y, orc.transform(amp, phase, u, v, -1, LAM)) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split32"])
+def test_const_phase_counts_sources(holo, prec):
+    """TEST_CONST_PHASE (cuda/superposition.cu:113-116): every term 1+0i, so y_m == N exactly,
+    through source splits, partial sums and the scatter back to caller order."""
+    amp, phase, u, v, _ = config1()
+    for n, m in ((4096, 65536), (4096, 300), (1000, 5000)):
+        y = holo.transform(amp[:n], phase[:n], u[:n], v[:m], -1, LAM, precision=prec,
+                           flags=holo.FLAG_CONST_PHASE)
+        assert np.all(y.real == n) and np.all(y.imag == 0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split32"])
+def test_deterministic(holo, prec):
+    amp, phase, u, v, _ = config1(seed=2)
+    a = holo.transform(amp, phase, u, v[:20000], -1, LAM, precision=prec)
+    b = holo.transform(amp, phase, u, v[:20000], -1, LAM, precision=prec)
+    assert np.array_equal(a, b)
+
+
+def test_config2_split_vs_fp64_kernel(holo, orc):
+    """Config 2 at full source count: split-FP32 vs the FP64 kernel (validated above against
+    the CPU oracle) on a seeded 4096-target subset, and vs the CPU oracle on 64 targets."""
+    import torch
+    amp, phase, u, v, _ = config2()
+    rng = np.random.default_rng(1)
+    idx = np.sort(rng.choice(len(v), 4096, replace=False))
+    ys = holo.transform(amp, phase, u, v[idx], -1, LAM, precision="split32")
+    yd = holo.transform(amp, phase, u, v[idx], -1, LAM, precision="fp64")
+    err = rel_l2(ys, yd)
+    print(f"config2 subset: rel-L2 {err:.3e}, max phase err {max_phase_err(ys, yd):.3e}")
+    assert err < 1e-5
+    yc = orc.transform_subset(amp, phase, u, v, idx[:64], -1, LAM)
+    assert rel_l2(yd[:64], yc) < 1e-12
+    # the full 2.75e11-pair pass runs on device buffers
+    dev = torch.device("cuda:0")
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+    y_full = holo.transform(t(amp), t(phase), t(u), t(v), -1, LAM, precision="split32")
+    torch.cuda.synchronize()
+    y_full = y_full.cpu().numpy()
+    assert rel_l2(y_full[idx], yd) < 1e-5
+
+
+def test_plan_reuse_and_orders(holo, orc):
+    amp, phase, u, v, _ = config1(seed=3)
+    with holo.Plan(u, v[:30000], "split32") as pl:
+        so, to = pl.order(0), pl.order(1)
+        assert np.array_equal(np.sort(so), np.arange(len(u)))
+        assert np.array_equal(np.sort(to), np.arange(30000))
+        for seed in range(2):
+            ph = np.random.default_rng(seed).uniform(0, 2 * np.pi, len(u))
+            y = pl.execute(amp, ph, -1, LAM)
+            assert rel_l2(y, orc.transform(amp, ph, u, v[:30000], -1, LAM)) < 1e-5
+
+
+def test_torch_device_path_is_async_and_matches(holo, orc):
+    import torch
+    amp, phase, u, v, _ = config1(seed=4)
+    dev = torch.device("cuda:0")
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+    y = holo.transform(t(amp), t(phase), t(u), t(v), -1, LAM, precision="split32")
+    assert y.is_cuda and y.dtype == torch.complex128
+    torch.cuda.synchronize()
+    assert rel_l2(y.cpu().numpy(), orc.transform(amp, phase, u, v, -1, LAM)) < 1e-5
+    holo.handle(0).status()
+
+
+def test_invalid_arguments_return_status(holo):
+    amp, phase, u, v, _ = config1()
+    with pytest.raises(holo.HoloError) as e:
+        holo.transform(amp, phase, u, v, 0, LAM)
+    assert e.value.code == -1
+    with pytest.raises(holo.HoloError):
+        holo.transform(amp, phase, u, v, -1, float("nan"))
+    with pytest.raises(holo.HoloError):
+        holo.transform(amp, phase, u, v, -1, LAM, precision="split32", variant=99)
+    import torch
+    with pytest.raises(holo.HoloError):  # mixed host and device pointers
+        holo.transform(torch.as_tensor(amp, device="cuda:0"), phase, u, v, -1, LAM)
+    holo.handle(0).status()  # nothing left on the device error word
+
+
+def test_reference_wave_amplitude_only(holo, orc):
+    """PROJECT_PHASE=0 path (cuda/transform.cu:379-395) restated with the oracle."""
+    amp, phase, u, v, _ = config1(seed=6)
+    u, amp, phase, v = u[:512], amp[:512], phase[:512], v[:8192]
+    ya, yp, _, _ = holo.project(amp, phase, u, v, None, LAM, precision="fp64",
+                                reference_wave=True, reference_distance=0.25)
+    y = orc.transform(amp, phase, u, v, -1, LAM)
+    src = np.array([[0.0, 0.0, v[0, 2] - 0.25]])
+    yr = orc.transform([1.0], [0.0], src, v, +1, LAM)
+    yn, _ = orc.normalize_amp(y)
+    rn, _ = orc.normalize_amp(yr)
+    expect_amp = np.abs(yn + rn)
+    expect_phase = np.angle(rn)
+    assert np.max(np.abs(ya - expect_amp)) < 1e-10
+    assert np.max(np.abs(np.angle(np.exp(1j * (yp - expect_phase))))) < 1e-10
