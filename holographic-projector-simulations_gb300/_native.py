@@ -55,6 +55,7 @@ SIGNATURES = {
     "holo_plan_execute_flags": (_i, [_vp, _i, _d, _dp, _dp, _dp, _i, _vp]),
     "holo_plan_get_order": (_i, [_vp, _i, _vp]),
     "holo_plan_info": (_i, [_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)]),
+    "holo_plan_error_bound": (_i, [_vp, _c.POINTER(_d)]),
     "holo_transform_mc": (_i, [_vp, _i, _d, _dp, _dp, _dp, _sz, _dp, _sz, _dp, _c.c_uint64, _i,
                                _i, _vp]),
     "holo_plan_execute_mc": (_i, [_vp, _i, _d, _dp, _dp, _dp, _c.c_uint64, _i, _i, _vp]),

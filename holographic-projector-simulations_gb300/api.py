@@ -353,8 +353,10 @@ class Plan:
         v, s, tt, cs = (ctypes.c_int() for _ in range(4))
         N.check(self.h.lib.holo_plan_info(self.p, ctypes.byref(v), ctypes.byref(s),
                                           ctypes.byref(tt), ctypes.byref(cs)))
+        b = ctypes.c_double()
+        N.check(self.h.lib.holo_plan_error_bound(self.p, ctypes.byref(b)))
         return {"variant": v.value, "splits": s.value, "target_tile": tt.value,
-                "source_tile": cs.value}
+                "source_tile": cs.value, "path_error_bound_m": b.value}
 
 
 # ---- batches ----------------------------------------------------------------------------

@@ -195,11 +195,10 @@ void plan_release(holo_plan_s *p, cudaStream_t s) {
   delete p;
 }
 
-static int build_tiling(holo_plan_s *p, const double *pos, int n, int tile, int n_pad,
-                        double **pos_sorted, double **tiles, int32_t **order, cudaStream_t s) {
-  const int n_tiles = (n + tile - 1) / tile;
+// Sort a point set into tile order (the order does not depend on the tile size).
+static int sort_set(holo_plan_s *p, const double *pos, int n, int n_pad, double **pos_sorted,
+                    int32_t **order, cudaStream_t s) {
   HOLO_TRY(alloc_plan(p, (void **)pos_sorted, (size_t)3 * std::max(n_pad, 1) * sizeof(double), s));
-  HOLO_TRY(alloc_plan(p, (void **)tiles, (size_t)6 * std::max(n_tiles, 1) * sizeof(double), s));
   HOLO_TRY(alloc_plan(p, (void **)order, (size_t)std::max(n, 1) * sizeof(int32_t), s));
   if (n == 0) return launch_gather_pos(pos, nullptr, 0, n_pad, *pos_sorted, s);
   Scratch tmp(p->h, s);
@@ -213,9 +212,57 @@ static int build_tiling(holo_plan_s *p, const double *pos, int n, int tile, int 
   HOLO_TRY(launch_bbox(pos, n, bbox, bscr, 1024, s));
   HOLO_TRY(sort_points(pos, n, bbox, *order, keys, hist, scan, s));
   HOLO_TRY(launch_gather_pos(pos, *order, n, n_pad, *pos_sorted, s));
-  HOLO_TRY(launch_tile_bbox(*pos_sorted, n, tile, *tiles, s));
   return HOLO_OK;
 }
+
+// Tile boxes for source tiles of `cs` and target tiles of `tt` points, and a
+// bound (in metres) on the error of the split-precision path length r:
+//   c = |d_perp|^2 <= (hs + ht)^2 over the worst tile pair, r >= gap between
+//   the two point sets' boxes, rho = c / 2r the FP32 curvature term:
+//   FP32 rounding of rho (~4 ulp), of the in-tile offsets (c / r * 2^-24) and
+//   the truncated series term rho (c / r^2)^2 / 8.
+static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, cudaStream_t s) {
+  const int ns = (p->N + cs - 1) / cs, nt = (p->M + tt - 1) / tt;
+  HOLO_TRY(launch_tile_bbox(p->pos_s, p->N, cs, p->tiles_s, s));
+  HOLO_TRY(launch_tile_bbox(p->pos_t, p->M, tt, p->tiles_t, s));
+  std::vector<double> ts((size_t)6 * ns), tg((size_t)6 * nt);
+  if (ns) HOLO_CUDA(cudaMemcpyAsync(ts.data(), p->tiles_s, ts.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (nt) HOLO_CUDA(cudaMemcpyAsync(tg.data(), p->tiles_t, tg.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  HOLO_CUDA(cudaStreamSynchronize(s));
+  auto boxes = [](const std::vector<double> &t, int n, double *lo, double *hi, double *hmax) {
+    for (int d = 0; d < 3; ++d) { lo[d] = 1e300; hi[d] = -1e300; }
+    *hmax = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double *c = &t[6 * (size_t)i];
+      double h2 = 0.0;
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = std::min(lo[d], c[d] - c[3 + d]);
+        hi[d] = std::max(hi[d], c[d] + c[3 + d]);
+        h2 += c[3 + d] * c[3 + d];
+      }
+      *hmax = std::max(*hmax, sqrt(h2));
+    }
+  };
+  double slo[3], shi[3], tlo[3], thi[3], hs, ht;
+  boxes(ts, ns, slo, shi, &hs);
+  boxes(tg, nt, tlo, thi, &ht);
+  double gap2 = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    const double g = std::max(0.0, std::max(slo[d] - thi[d], tlo[d] - shi[d]));
+    gap2 += g * g;
+  }
+  const double gap = sqrt(gap2);
+  if (!(gap > 0.0) || ns == 0 || nt == 0) {
+    *bound = ns && nt ? INFINITY : 0.0;
+    return HOLO_OK;
+  }
+  const double c = (hs + ht) * (hs + ht), rho = c / (2.0 * gap), y = c / gap2;
+  *bound = rho * ldexp(1.0, -21) + c / gap * ldexp(1.0, -24) + rho * y * y / 8.0;
+  return HOLO_OK;
+}
+
+// Path-length error budget of the split path: 5e-6 rad at lambda = 400 nm.
+constexpr double kSplitBoundMetres = 5e-6 * 400e-9 / (2.0 * M_PI);
 
 int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, size_t M,
                      int precision, int forced_variant, cudaStream_t s, holo_plan_s **out) {
@@ -229,16 +276,42 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
   p->M = (int)M;
   p->last_stream = s;
   const int bucket = size_bucket(N, M);
+  const int nv = precision == HOLO_SPLIT32 ? split_variant_count() : fp64_variant_count();
+  if (forced_variant >= nv) return fail(HOLO_ERR_INVALID, "variant %d out of range", forced_variant);
   int variant = forced_variant;
   if (variant < 0) variant = h->variant_table[precision][bucket];
   if (variant < 0)
     variant = precision == HOLO_SPLIT32 ? default_split_variant(N, M) : default_fp64_variant(N, M);
-  const int nv = precision == HOLO_SPLIT32 ? split_variant_count() : fp64_variant_count();
-  if (variant >= nv) return fail(HOLO_ERR_INVALID, "variant %d out of range", variant);
+
+  if (precision == HOLO_SPLIT32) {
+    // sort once; pad sources to a multiple of every source tile size
+    p->n_pad = std::max<int>(1, (int)((N + 1023) / 1024)) * 1024;
+    HOLO_TRY(sort_set(p.get(), u, (int)N, p->n_pad, &p->pos_s, &p->order_s, s));
+    HOLO_TRY(sort_set(p.get(), v, (int)M, (int)M, &p->pos_t, &p->order_t, s));
+    HOLO_TRY(alloc_plan(p.get(), (void **)&p->tiles_s, (size_t)6 * (N / 256 + 1) * sizeof(double), s));
+    HOLO_TRY(alloc_plan(p.get(), (void **)&p->tiles_t, (size_t)6 * (M / 256 + 1) * sizeof(double), s));
+    // candidates: the chosen variant, then ever smaller tiles until the
+    // path-length error bound holds (sparse or wide point sets need small tiles)
+    std::vector<int> cands = {variant};
+    if (forced_variant < 0)
+      for (int c : {0, 2, 3, 4})
+        if (split_variant(c).tt() < split_variant(variant).tt() ||
+            (split_variant(c).tt() == split_variant(variant).tt() &&
+             split_variant(c).cs < split_variant(variant).cs))
+          cands.push_back(c);
+    for (size_t i = 0; i < cands.size(); ++i) {
+      const Variant C = split_variant(cands[i]);
+      double bound = 0.0;
+      HOLO_TRY(tile_error_bound(p.get(), C.cs, C.tt(), &bound, s));
+      variant = cands[i];
+      p->err_bound = bound;
+      if (bound <= kSplitBoundMetres) break;
+    }
+  }
   const Variant V = precision == HOLO_SPLIT32 ? split_variant(variant) : fp64_variant(variant);
   p->variant = variant;
   p->n_stiles = (int)((N + V.cs - 1) / V.cs);
-  p->n_pad = std::max(p->n_stiles, 1) * V.cs;
+  if (precision != HOLO_SPLIT32) p->n_pad = std::max(p->n_stiles, 1) * V.cs;
   p->n_ttiles = (int)((M + V.tt() - 1) / V.tt());
 
   int occ = 0;
@@ -253,12 +326,7 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
   p->splits = choose_splits(p->n_ttiles, p->n_stiles, G, M, max_splits);
   p->grid = std::max(1, std::min(G, p->n_ttiles * p->splits));
 
-  if (precision == HOLO_SPLIT32) {
-    HOLO_TRY(build_tiling(p.get(), u, (int)N, V.cs, p->n_pad, &p->pos_s, &p->tiles_s,
-                          &p->order_s, s));
-    HOLO_TRY(build_tiling(p.get(), v, (int)M, V.tt(), (int)M, &p->pos_t, &p->tiles_t,
-                          &p->order_t, s));
-  } else {
+  if (precision != HOLO_SPLIT32) {
     HOLO_TRY(alloc_plan(p.get(), (void **)&p->pos_s, (size_t)3 * p->n_pad * sizeof(double), s));
     HOLO_TRY(alloc_plan(p.get(), (void **)&p->pos_t, (size_t)3 * std::max<size_t>(M, 1) * sizeof(double), s));
     HOLO_TRY(launch_pack_pos(u, (int)N, p->n_pad, p->pos_s, s));
@@ -356,9 +424,6 @@ static int plan_execute_mc_impl(holo_plan_s *p, int sign, double lambda, const d
   if (sub < 1) return fail(HOLO_ERR_INVALID, "subsample must be >= 1");
   const int v = mc_variant_for_block(block);
   if (v < 0) return fail(HOLO_ERR_INVALID, "targets_per_block %d: use 256, 512, 1024 or 2048", block);
-  if (v != p->variant)
-    return fail(HOLO_ERR_INVALID, "plan variant %d has target tile %d, not %d", p->variant,
-                split_variant(p->variant).tt(), block);
   p->last_stream = s;
   if (p->M == 0) return HOLO_OK;
   if (p->N == 0) {
@@ -366,38 +431,50 @@ static int plan_execute_mc_impl(holo_plan_s *p, int sign, double lambda, const d
     return HOLO_OK;
   }
   const Variant V = split_variant(v);
+  const int n_stiles = (p->N + V.cs - 1) / V.cs, n_ttiles = (p->M + V.tt() - 1) / V.tt();
   const int n_strata = (p->N + sub - 1) / sub;
   const int n_chunks = (n_strata + V.cs - 1) / V.cs;
   int occ = 0;
   HOLO_TRY(split_occupancy(v, true, &occ));
   const int G = std::max(1, occ) * p->h->sm_count;
   const int max_splits = (int)std::max<size_t>(1, ((size_t)1 << 30) / ((size_t)p->M * 16));
-  const int splits = choose_splits(p->n_ttiles, n_chunks, G, p->M, max_splits);
+  const int splits = choose_splits(n_ttiles, n_chunks, G, p->M, max_splits);
   Scratch tmp(p->h, s);
   double2 *ap = tmp.get<double2>(p->n_pad);
   double2 *partial = splits > 1 ? tmp.get<double2>((size_t)splits * p->M) : nullptr;
   if (!ap || (splits > 1 && !partial)) return fail(HOLO_ERR_ALLOC, "execute scratch");
+  // tile boxes for the Monte Carlo block size when the plan was tiled differently
+  const double *tiles_s = p->tiles_s, *tiles_t = p->tiles_t;
+  if (v != p->variant) {
+    double *ts = tmp.get<double>((size_t)6 * n_stiles);
+    double *tt = tmp.get<double>((size_t)6 * n_ttiles);
+    if (!ts || !tt) return fail(HOLO_ERR_ALLOC, "execute scratch");
+    HOLO_TRY(launch_tile_bbox(p->pos_s, p->N, V.cs, ts, s));
+    HOLO_TRY(launch_tile_bbox(p->pos_t, p->M, V.tt(), tt, s));
+    tiles_s = ts;
+    tiles_t = tt;
+  }
   HOLO_TRY(launch_gather_ap(amp, phase, p->order_s, p->N, p->n_pad, ap, s));
   SplitProblem P{};
   P.pos_s = p->pos_s;
   P.ap_s = ap;
-  P.tiles_s = p->tiles_s;
+  P.tiles_s = tiles_s;
   P.pos_t = p->pos_t;
-  P.tiles_t = p->tiles_t;
+  P.tiles_t = tiles_t;
   P.order_t = p->order_t;
   P.partial = partial;
   P.y = y;
   P.N = p->N;
   P.M = p->M;
-  P.n_stiles = p->n_stiles;
-  P.n_ttiles = p->n_ttiles;
+  P.n_stiles = n_stiles;
+  P.n_ttiles = n_ttiles;
   P.splits = splits;
   P.sign = sign;
   P.sk = sign * ((2.0 * M_PI) / lambda);
   P.seed_lo = (uint32_t)seed;
   P.seed_hi = (uint32_t)(seed >> 32);
   P.sub = sub;
-  const int grid = std::max(1, std::min(G, p->n_ttiles * splits));
+  const int grid = std::max(1, std::min(G, n_ttiles * splits));
   HOLO_TRY(profile_mark(p->h, s, true));
   HOLO_TRY(launch_split(P, v, grid, false, true, p->h->dev_err, s));
   HOLO_TRY(profile_mark(p->h, s, false));
@@ -531,6 +608,12 @@ int holo_plan_info(holo_plan p, int *variant, int *splits, int *target_tile, int
   if (splits) *splits = p->splits;
   if (target_tile) *target_tile = V.tt();
   if (source_tile) *source_tile = V.cs;
+  return HOLO_OK;
+}
+
+int holo_plan_error_bound(holo_plan p, double *metres) {
+  if (!p || !metres) return fail(HOLO_ERR_INVALID, "null argument");
+  *metres = p->precision == HOLO_SPLIT32 ? p->err_bound : 0.0;
   return HOLO_OK;
 }
 

@@ -177,6 +177,7 @@ struct holo_plan_s {
   int splits = 1;
   int grid = 0;
   int n_stiles = 0, n_ttiles = 0;
+  double err_bound = 0.0;        // split path: bound on the path-length error (m)
   cudaStream_t last_stream = nullptr;
   // device buffers
   double *pos_s = nullptr;       // 3 * n_pad

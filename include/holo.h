@@ -111,6 +111,12 @@ int holo_plan_get_order(holo_plan p, int which, int32_t *out);
 /* Selected kernel variant and split factor (for the autotuner and tests). */
 int holo_plan_info(holo_plan p, int *variant, int *splits, int *target_tile,
                    int *source_tile);
+/* HOLO_SPLIT32: bound (metres) on the path-length error of any term, from the
+ * tile extents and the gap between the point sets; the phase error bound is
+ * k times it.  The planner picks tiles small enough to keep it under 3.2e-13 m
+ * (5e-6 rad at 400 nm) when it can; 0 for HOLO_FP64.  Infinite when the two
+ * point sets' bounding boxes touch (near field: use HOLO_FP64). */
+int holo_plan_error_bound(holo_plan p, double *metres);
 
 /* ---- Monte Carlo estimator (transform(), README.md:127; not in the snapshot)
  * Sources in tile order are cut into strata of `subsample` entries, targets in

@@ -1,0 +1,259 @@
+"""GPU tests of the extensions around the hot path: Monte Carlo estimator,
+adjoint (autograd), batched persistent launch, and the reference-compatible CLI."""
+import json
+import math
+import os
+import subprocess
+import time
+
+import numpy as np
+import pytest
+
+from conftest import LAM, config1, grid, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+# ---- Monte Carlo (config 3) ------------------------------------------------------------
+def test_mc_matches_oracle_restatement(holo, orc):
+    """Same strata, blocks and Philox picks as the oracle, given the plan's tile orders."""
+    amp, phase, u, v, _ = config1()
+    v = v[:16384]
+    with holo.Plan(u, v, "split32") as pl:
+        so, to = pl.order(0), pl.order(1)
+        for sub in (16, 5):
+            y = pl.execute_mc(amp, phase, -1, LAM, seed=123, subsample=sub, targets_per_block=256)
+            ref = orc.transform_mc(amp, phase, u, v, -1, LAM, so, to, seed=123, sub=sub, block=256)
+            assert rel_l2(y, ref) < 1e-5
+
+
+def test_mc_full_sampling_is_brute_force(holo, orc):
+    amp, phase, u, v, _ = config1()
+    v = v[:8192]
+    y = holo.transform_mc(amp, phase, u, v, -1, LAM, seed=1, subsample=1, targets_per_block=256)
+    assert rel_l2(y, orc.transform(amp, phase, u, v, -1, LAM)) < 1e-5
+
+
+def test_mc_config3_error_and_unbiasedness(holo, orc):
+    """Config 3: 1/16 of the sources per block of 256 targets, x16 (report rel-L2)."""
+    amp, phase, u, v, _ = config1()
+    v = v[:4096]
+    ref = orc.transform(amp, phase, u, v, -1, LAM)
+    runs = np.array([holo.transform_mc(amp, phase, u, v, -1, LAM, seed=s, subsample=16,
+                                       targets_per_block=256) for s in range(64)])
+    single = np.mean([rel_l2(r, ref) for r in runs])
+    mean_err = rel_l2(runs.mean(0), ref)
+    print(f"config3: MC rel-L2 single {single:.3f}, mean of 64 {mean_err:.3f}")
+    assert mean_err < 2.0 * single / math.sqrt(64)
+
+
+# ---- adjoint (config 5) -----------------------------------------------------------------
+def _small_problem(seed=0, n=256, m=4096):
+    import torch
+    rng = np.random.default_rng(seed)
+    u = grid(16, 7.56e-6, 0.0)[:n]
+    v = grid(64, 10e-6, 0.35)[:m]
+    amp = rng.uniform(0.5, 1.0, n)
+    phase = rng.uniform(0, 2 * np.pi, n)
+    target = rng.uniform(0, 2, m)
+    dev = torch.device("cuda:0")
+    T = lambda a: torch.as_tensor(a, dtype=torch.float64, device=dev)
+    return T(amp), T(phase), T(u), T(v), T(target)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-9), ("split32", 1e-4)])
+def test_adjoint_matches_dense_autograd(holo, prec, tol):
+    import torch
+    from holo_gb300 import torch_ops
+    amp, phase, u, v, target = _small_problem()
+    a1 = amp.clone().requires_grad_(True)
+    p1 = phase.clone().requires_grad_(True)
+    z = torch_ops.dense_reference(a1, p1, u, v, +1, LAM)
+    torch_ops.intensity_loss(z, target).backward()
+    a2 = amp.clone().requires_grad_(True)
+    p2 = phase.clone().requires_grad_(True)
+    with holo.Plan(u.reshape(-1), v.reshape(-1), prec) as pl:
+        z2 = torch_ops.huygens(a2, p2, pl, +1, LAM)
+        assert rel_l2(z2.detach().cpu(), z.detach().cpu()) < max(tol, 1e-11)
+        torch_ops.intensity_loss(z2, target).backward()
+    assert rel_l2(p2.grad.cpu(), p1.grad.cpu()) < tol
+    assert rel_l2(a2.grad.cpu(), a1.grad.cpu()) < tol
+
+
+def test_adjoint_central_differences(holo):
+    """dL/dphi against FP64 central differences (h = 1e-3) on 64 random phases."""
+    import torch
+    from holo_gb300 import torch_ops
+    amp, phase, u, v, target = _small_problem(seed=1)
+    with holo.Plan(u.reshape(-1), v.reshape(-1), "fp64") as pl:
+        p = phase.clone().requires_grad_(True)
+        torch_ops.intensity_loss(torch_ops.huygens(amp, p, pl, +1, LAM), target).backward()
+        g = p.grad.cpu().numpy()
+        rng = np.random.default_rng(2)
+        idx = rng.choice(len(g), 64, replace=False)
+        h = 1e-3
+        fd = []
+        for i in idx:
+            pp, pm = phase.clone(), phase.clone()
+            pp[i] += h
+            pm[i] -= h
+            lp = float(torch_ops.intensity_loss(torch_ops.huygens(amp, pp, pl, +1, LAM), target))
+            lm = float(torch_ops.intensity_loss(torch_ops.huygens(amp, pm, pl, +1, LAM), target))
+            fd.append((lp - lm) / (2 * h))
+    fd = np.array(fd)
+    assert rel_l2(g[idx], fd) < 1e-5
+
+
+def test_adjoint_cost_ratio(holo):
+    """Backward (adjoint) costs <= 2.5x the forward pass at a size where kernels dominate."""
+    import torch
+    from holo_gb300 import torch_ops
+    dev = torch.device("cuda:0")
+    u = torch.as_tensor(grid(512, 7.56e-6, 0.0), device=dev).reshape(-1)
+    v = torch.as_tensor(grid(256, 10e-6, 0.35), device=dev).reshape(-1)
+    n = u.numel() // 3
+    amp = torch.ones(n, dtype=torch.float64, device=dev)
+    phase = torch.rand(n, dtype=torch.float64, device=dev) * 2 * math.pi
+    with holo.Plan(u, v, "split32") as pl:
+        g = torch.randn(v.numel() // 3, 2, dtype=torch.float64, device=dev)
+        for _ in range(2):
+            pl.execute(amp, phase, +1, LAM)
+            pl.adjoint(amp, phase, g, +1, LAM)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            pl.execute(amp, phase, +1, LAM)
+        torch.cuda.synchronize()
+        fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for _ in range(3):
+            pl.adjoint(amp, phase, g, +1, LAM)
+        torch.cuda.synchronize()
+        bwd = time.perf_counter() - t0
+    print(f"adjoint/forward time ratio {bwd / fwd:.2f}")
+    assert bwd / fwd <= 2.5
+
+
+def test_phase_hologram_optimisation_decreases_loss(holo):
+    import torch
+    from holo_gb300 import torch_ops
+    dev = torch.device("cuda:0")
+    pp = torch.as_tensor(grid(128, 7.56e-6, 0.0), device=dev)
+    tp = torch.as_tensor(grid(64, 10e-6, 0.35), device=dev)
+    rng = np.random.default_rng(0)
+    yy, xx = np.meshgrid(np.arange(64), np.arange(64), indexing="ij")
+    img = sum(rng.uniform(0.2, 1) * np.exp(-((xx - rng.uniform(0, 64)) ** 2 +
+                                            (yy - rng.uniform(0, 64)) ** 2) / (2 * 4.0 ** 2))
+              for _ in range(8)).ravel()
+    target = torch.as_tensor(img / img.mean(), device=dev)
+    _, losses = torch_ops.optimise_phase_hologram(pp, tp, target, LAM, steps=30, lr=0.05)
+    assert losses[-1] < 0.7 * losses[0]
+
+
+# ---- batched persistent launch (config 4) -------------------------------------------------
+def test_batched_matches_individual(holo, orc):
+    import torch
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(9)
+    probs, host = [], []
+    for i in range(7):
+        ns = int(np.exp(rng.uniform(np.log(1024), np.log(65536))))
+        side = int(math.ceil(math.sqrt(ns)))
+        u = grid(side, 10e-6, rng.uniform(0.2, 0.5))[:ns]
+        mside = [128, 256][i % 2]
+        v = grid(mside, 7.56e-6, 0.0)
+        amp, phase = rng.uniform(0, 1, ns), rng.uniform(0, 2 * np.pi, ns)
+        T = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+        y = torch.zeros(2 * len(v), dtype=torch.float64, device=dev)
+        sign = -1 if i % 3 else 1
+        probs.append(holo.Problem(T(amp), T(phase), T(u), T(v), sign, LAM, y))
+        host.append((amp, phase, u, v, sign))
+    with holo.Batch(probs, "split32") as b:
+        b.execute()
+        torch.cuda.synchronize()
+        b.execute()  # replay of the captured graph
+        torch.cuda.synchronize()
+        assert b.pairs == sum(len(h[0]) * len(h[3]) for h in host)
+    for pb, (amp, phase, u, v, sign) in zip(probs, host):
+        yb = pb.y.cpu().numpy().view(np.complex128)
+        yi = holo.transform(amp, phase, u, v, sign, LAM, precision="split32")
+        assert rel_l2(yb, yi) < 1e-6
+        idx = np.arange(0, len(v), 97)
+        assert rel_l2(yb[idx], orc.transform_subset(amp, phase, u, v, idx, sign, LAM)) < 1e-5
+    holo.handle(0).status()
+
+
+# ---- CLI: the reference's file interface ---------------------------------------------------
+def _cli(holo):
+    return os.path.join(os.path.dirname(holo.__file__), "holo")
+
+
+def test_cli_file_mode_chain(holo, orc, tmp_path):
+    rng = np.random.default_rng(21)
+    u = grid(16, 10e-6, 0.35)
+    v = grid(48, 7.56e-6, 0.0)
+    w = grid(16, 10e-6, 0.35)
+    amp, phase = rng.uniform(0, 1, len(u)), rng.uniform(0, 2 * np.pi, len(u))
+    holo.io.write_inputs(str(tmp_path), amp, phase, u, v, w)
+    r = subprocess.run([_cli(holo), "-f", str(tmp_path), "-F", "--lambda", str(LAM)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    y = orc.transform(amp, phase, u, v, -1, LAM)
+    yn, _ = orc.normalize_amp(y)
+    ya, yp = orc.to_polar(yn)
+    got_a = holo.io.read_dat(str(tmp_path / "y0_amp.dat"))
+    got_p = holo.io.read_dat(str(tmp_path / "y0_phase.dat"))
+    assert np.max(np.abs(got_a - ya)) < 1e-12
+    assert rel_l2(got_a * np.exp(1j * got_p), ya * np.exp(1j * yp)) < 1e-12
+    z = orc.transform(ya, yp, v, w, +1, LAM)
+    zn, _ = orc.normalize_amp(z)
+    za, zp = orc.to_polar(zn)
+    got_za = holo.io.read_dat(str(tmp_path / "z0_0_amp.dat"))
+    got_zp = holo.io.read_dat(str(tmp_path / "z0_0_phase.dat"))
+    assert rel_l2(got_za * np.exp(1j * got_zp), za * np.exp(1j * zp)) < 1e-11
+    assert np.array_equal(holo.io.read_dat(str(tmp_path / "v0.dat")), v.ravel())
+    assert np.array_equal(holo.io.read_dat(str(tmp_path / "w0_0.dat")), w.ravel())
+    meta = holo.io.parse_out_json(str(tmp_path / "out.json"))
+    assert [m["phasor"] for m in meta] == ["y0", "z0_0"]
+    assert [m["pos"] for m in meta] == ["v0", "w0_0"]
+    assert meta[0]["len"] == len(v) and meta[0]["dims"] == 3 and meta[0]["precision"] == 8
+    assert meta[0]["amp_sum"] == pytest.approx(np.sum(got_a), rel=1e-5)
+    for k in ("phase_sum", "x_offset", "width", "randomized", "aspect_ratio", "timestamp",
+              "runtime", "flops"):
+        assert k in meta[0]
+
+
+def test_cli_ref_compat_and_w0_fallback(holo, orc, tmp_path):
+    rng = np.random.default_rng(22)
+    u = grid(8, 10e-6, 0.35)
+    v = grid(24, 7.56e-6, 0.0)
+    amp, phase = rng.uniform(0, 1, len(u)), rng.uniform(0, 2 * np.pi, len(u))
+    holo.io.write_inputs(str(tmp_path), amp, phase, u, v)
+    holo.io.write_dat(str(tmp_path / "w0.dat"), grid(8, 10e-6, 0.35))  # the reference's name
+    r = subprocess.run([_cli(holo), "-f", str(tmp_path), "-F", "--ref-compat", "--lambda",
+                        str(LAM)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    # the reference's -F: z from x at u onto v, Forwards (cuda/main.cu:219)
+    z = orc.transform(amp, phase, u, v, +1, LAM)
+    zn, _ = orc.normalize_amp(z)
+    za, _ = orc.to_polar(zn)
+    assert np.max(np.abs(holo.io.read_dat(str(tmp_path / "z0_0_amp.dat")) - za)) < 1e-12
+
+
+def test_cli_generated_mode(holo, tmp_path):
+    r = subprocess.run([_cli(holo), "-x", "16", "-y", "4096", "-z", "1024", "-Z", "2",
+                        "--out", str(tmp_path), "--precision", "split32"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    meta = holo.io.parse_out_json(str(tmp_path / "out.json"))
+    assert [m["phasor"] for m in meta] == ["x0", "y0", "z0_0", "z0_1"]
+    ya = holo.io.read_dat(str(tmp_path / "y0_amp.dat"))
+    assert ya.size == 4096 and ya.max() == pytest.approx(1.0)
+    u = holo.io.read_dat(str(tmp_path / "u0.dat")).reshape(-1, 3)
+    assert np.allclose(u[:, 2], 0.35) and np.allclose(np.hypot(u[:, 0], u[:, 1]), 0.5e-3)
+
+
+def test_cli_rejects_bad_files(holo, tmp_path):
+    holo.io.write_inputs(str(tmp_path), [1.0, 2.0], [0.0], [0, 0, 1, 0, 0, 1], [0, 0, 0])
+    r = subprocess.run([_cli(holo), "-f", str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 2 and "inconsistent" in r.stderr
