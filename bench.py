@@ -190,6 +190,25 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_case(args):
+    """Two launches of the pair kernel on a config-2 slice (the second is the one to capture)."""
+    import torch
+    import __graft_entry__ as entry
+    entry._load_build_module().build()
+    holo = entry.load_package()
+    amp, phase, u, v, _ = workload()
+    side = 1024
+    vv = v.reshape(side, side, 3)[384:640, 384:640].reshape(-1, 3)  # central 256^2 patch
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+    args_ = (t(amp), t(phase), t(u), t(vv))
+    with holo.Plan(args_[2], args_[3], args.precision) as pl:
+        for _ in range(2):
+            pl.execute(args_[0], args_[1], -1, LAM)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": pl.info(), "pairs_per_launch": len(amp) * len(vv)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -198,9 +217,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="split32", choices=["split32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu: two split-FP32 passes of the 512^2 sources onto "
+                         "a 256^2 patch of the projector (1.7e10 pairs each), then exit")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_case:
+        return run_profile_case(args)
 
     import torch
     import torch.distributed as dist

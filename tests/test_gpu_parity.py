@@ -157,9 +157,14 @@ def test_torch_device_path_is_async_and_matches(holo, orc):
 
 def test_invalid_arguments_return_status(holo):
     amp, phase, u, v, _ = config1()
-    with pytest.raises(holo.HoloError) as e:
+    with pytest.raises(ValueError):  # the Python layer rejects it first
         holo.transform(amp, phase, u, v, 0, LAM)
-    assert e.value.code == -1
+    lib, h = holo._native.load(), holo.handle(0)
+    a, p, uu, vv = (np.ascontiguousarray(x) for x in (amp, phase, u, v))
+    y = np.zeros(2 * len(v))
+    rc = lib.holo_transform(h.h, 0, LAM, a.ctypes.data, p.ctypes.data, uu.ctypes.data, len(a),
+                            vv.ctypes.data, len(v), y.ctypes.data, 1, None)
+    assert rc == -1 and b"sign" in lib.holo_last_error_string()
     with pytest.raises(holo.HoloError):
         holo.transform(amp, phase, u, v, -1, float("nan"))
     with pytest.raises(holo.HoloError):
