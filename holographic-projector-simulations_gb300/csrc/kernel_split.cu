@@ -3,8 +3,9 @@
 // Reference hot path: superposition::per_block + phasor_displacement
 // (cuda/superposition.cu:35-51, 59-154) in FP64.  Here each CTA owns a tile of
 // TT = THREADS * R targets (R per thread, in registers) and walks source tiles
-// of CS points that a TMA bulk copy stages in shared memory (double-buffered,
-// mbarrier-tracked).  For every (target tile, source tile) pair a frame is
+// of CS points that a TMA bulk copy stages in shared memory (mbarrier-tracked;
+// the copy of the next tile overlaps the current pair loop).  For every
+// (target tile, source tile) pair a frame is
 // built in FP64 from the two tile centres T0, S0:
 //   D = T0 - S0, r0 = |D|, e = D / r0, (e1, e2) an orthonormal basis of e-perp.
 // With t' = t - T0, s' = s - S0 and d = t' - s':
@@ -87,11 +88,13 @@ __device__ __forceinline__ void build_frame(Frame *fr, const double *t0, const d
   fr->b0 = reduce_two_pi(sk * r0);
 }
 
+// One raw (FP64) staging buffer: the bulk copy of tile j+1 is issued once the
+// frame phase of tile j has consumed it, so it overlaps tile j's pair loop.
 template <int THREADS, int R, int CS>
 struct SplitSmem {
-  static constexpr size_t raw_pos = 0;                                   // double [2][CS*3]
-  static constexpr size_t raw_ap = raw_pos + 2 * CS * 3 * sizeof(double);  // double2 [2][CS]
-  static constexpr size_t rec = raw_ap + 2 * CS * sizeof(double2);        // float4 [CS]
+  static constexpr size_t raw_pos = 0;                                   // double [CS*3]
+  static constexpr size_t raw_ap = raw_pos + CS * 3 * sizeof(double);    // double2 [CS]
+  static constexpr size_t rec = raw_ap + CS * sizeof(double2);           // float4 [CS]
   static constexpr size_t amp = rec + CS * sizeof(float4);                // float [CS]
   static constexpr size_t acc = (amp + CS * sizeof(float) + 15) / 16 * 16;  // double2 [R][THREADS]
   static constexpr size_t bphase = acc + R * THREADS * sizeof(double2);      // float [R][THREADS]
@@ -124,23 +127,22 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
   const float kap8 = (float)(0.125 * sk);  // s k / 8
   const int n_strata = MC ? (P.N + P.sub - 1) / P.sub : 0;
 
-  auto issue = [&](int j, int buf) {
+  auto issue = [&](int j) {
     // tile j of CS sources: CS*24 B of positions + CS*16 B of (phase, amp)
-    ptx::mbar_arrive_expect_tx(&bar[buf], CS * (3 * sizeof(double) + sizeof(double2)));
-    ptx::bulk_g2s(raw_pos + buf * CS * 3, P.pos_s + (size_t)j * CS * 3,
-                  CS * 3 * sizeof(double), &bar[buf]);
-    ptx::bulk_g2s(raw_ap + buf * CS, P.ap_s + (size_t)j * CS, CS * sizeof(double2),
-                  &bar[buf]);
+    ptx::mbar_arrive_expect_tx(&bar[0], CS * (3 * sizeof(double) + sizeof(double2)));
+    ptx::bulk_g2s(raw_pos, P.pos_s + (size_t)j * CS * 3, CS * 3 * sizeof(double), &bar[0]);
+    ptx::bulk_g2s(raw_ap, P.ap_s + (size_t)j * CS, CS * sizeof(double2), &bar[0]);
   };
+  (void)par1;
 
-  if (!MC && tid == 0 && sb < se) issue(sb, 0);
+  if (!MC && tid == 0 && sb < se) issue(sb);
 
 #pragma unroll
   for (int r = 0; r < R; ++r) acc[r * THREADS + tid] = make_double2(0.0, 0.0);
 
   for (int j = sb; j < se; ++j) {
-    const int buf = (j - sb) & 1;
-    if (!MC && tid == 0 && j + 1 < se) issue(j + 1, buf ^ 1);
+    // sources with records in this tile (the pair loop skips the padding)
+    const int count = MC ? min(CS, n_strata - j * CS) : min(CS, P.N - j * CS);
     if (tid == 0) {
       const double *tc = P.tiles_t + 6 * (size_t)tt;
       double sc[3];
@@ -162,9 +164,8 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       build_frame(fr, tc, sc, sk);
     }
     if (!MC) {
-      const uint32_t par = buf ? par1 : par0;
-      const bool ok = ptx::mbar_wait_bounded(&bar[buf], par, kWaitCycles);
-      if (buf) par1 ^= 1u; else par0 ^= 1u;
+      const bool ok = ptx::mbar_wait_bounded(&bar[0], par0, kWaitCycles);
+      par0 ^= 1u;
       if (!__syncthreads_and(ok)) {
         if (tid == 0) atomicExch(err, kDevErrTimeout);
         return false;
@@ -182,8 +183,8 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       double sx, sy, sz, ph, am;
       if (!MC) {
         valid = j * CS + i < P.N;
-        const double *sp = raw_pos + buf * CS * 3 + 3 * i;
-        const double2 a2 = raw_ap[buf * CS + i];
+        const double *sp = raw_pos + 3 * i;
+        const double2 a2 = raw_ap[i];
         sx = sp[0]; sy = sp[1]; sz = sp[2];
         ph = a2.x; am = a2.y;
       } else {
@@ -244,8 +245,10 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       bph[r * THREADS + tid] = (float)B;
     }
     __syncthreads();
+    // the staging buffer is free: fetch the next tile while this one is summed
+    if (!MC && tid == 0 && j + 1 < se) issue(j + 1);
 
-    // ---- pair loop: CS sources x R targets ----
+    // ---- pair loop: count sources x R targets ----
     float re[R], im[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -253,7 +256,7 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       im[r] = 0.f;
     }
 #pragma unroll 2
-    for (int s = 0; s < CS; ++s) {
+    for (int s = 0; s < count; ++s) {
       const float4 q = rec[s];
       const float a = ramp[s];
       if (CONST) {
@@ -367,12 +370,12 @@ __global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
 
 // ---- variant table ------------------------------------------------------------
 constexpr Variant kVariants[] = {
-    {256, 8, 512},  // 0: TT 2048
-    {128, 8, 512},  // 1: TT 1024
-    {256, 4, 512},  // 2: TT 1024
-    {128, 4, 256},  // 3: TT 512
+    {256, 8, 1024}, // 0: TT 2048
+    {128, 8, 1024}, // 1: TT 1024
+    {256, 4, 1024}, // 2: TT 1024
+    {128, 4, 512},  // 3: TT 512
     {128, 2, 256},  // 4: TT 256 (Monte Carlo blocks of 256 targets)
-    {256, 8, 1024}, // 5: TT 2048, long source tiles
+    {256, 8, 512},  // 5: TT 2048, short source tiles
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -427,12 +430,12 @@ Variant split_variant(int i) { return kVariants[i]; }
 
 #define HOLO_SPLIT_DISPATCH(V, CALL)                      \
   switch (V) {                                            \
-    case 0: return CALL(256, 8, 512);                     \
-    case 1: return CALL(128, 8, 512);                     \
-    case 2: return CALL(256, 4, 512);                     \
-    case 3: return CALL(128, 4, 256);                     \
+    case 0: return CALL(256, 8, 1024);                     \
+    case 1: return CALL(128, 8, 1024);                     \
+    case 2: return CALL(256, 4, 1024);                     \
+    case 3: return CALL(128, 4, 512);                     \
     case 4: return CALL(128, 2, 256);                     \
-    case 5: return CALL(256, 8, 1024);                    \
+    case 5: return CALL(256, 8, 512);                    \
     default: return fail(HOLO_ERR_INVALID, "unknown split variant %d", V); \
   }
 
