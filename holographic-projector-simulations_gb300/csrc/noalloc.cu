@@ -1,0 +1,282 @@
+// noalloc.cu -- holo_transform_noalloc: the split-precision transform for
+// callers that cannot allocate GPU memory.
+//
+// Who needs it: code that runs where a cudaMalloc (or a memory-pool call)
+// is not allowed or not safe -- a host application that hands the library a
+// fixed memory budget and owns every byte on the device, a plugin loaded into
+// a process whose allocator must not be bypassed, a real-time loop that must
+// not hit the implicit device synchronisation of cudaMalloc/cudaFree, or a
+// context that must not grow its footprint after start-up.  Such a caller
+// passes its own device buffers for the inputs and the output; every other
+// byte this transform needs (tile-ordered positions, gathered amplitudes,
+// tile boxes, sort scratch, cross-CTA partial sums, the error word) comes from
+// one fixed array below, reserved when the library's device code is loaded
+// on a GPU and held until the process exits.
+//
+// Limits and rules:
+//   - the array is kNoAllocBytes (64 MiB); a call whose problem does not fit
+//     is rejected with HOLO_ERR_INVALID and a message giving the bytes needed;
+//   - all calls on a device share the array and each call overwrites it: two
+//     calls that overlap on the GPU would race.  Calls in this process are
+//     serialised by a lock and each call returns only after its work on
+//     `stream` has finished;
+//   - the first call on a device looks up the array's device address with
+//     cudaGetSymbolAddress (with that device current); make that first call
+//     before any stream capture.
+//   - no cudaMalloc, cudaFree, memory-pool or allocating library routine is
+//     called on this path.
+#include <math.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "internal.cuh"
+
+namespace holo {
+namespace {
+
+constexpr size_t kNoAllocBytes = (size_t)64 << 20;
+constexpr int kMaxDevices = 64;
+
+// The scratch of every holo_transform_noalloc call on this device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of the array on `device` (looked up once per device).
+int noalloc_scratch(int device, unsigned char **out) {
+  if (device < 0 || device >= kMaxDevices) return fail(HOLO_ERR_INVALID, "device %d out of range", device);
+  if (!g_noalloc_addr[device]) {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)", __FILE__, __LINE__);
+    g_noalloc_addr[device] = ptr;
+  }
+  *out = static_cast<unsigned char *>(g_noalloc_addr[device]);
+  return HOLO_OK;
+}
+
+// Reduce the tile boxes of both point sets to 14 numbers: source box lo/hi,
+// largest source tile half-diagonal, target box lo/hi, largest target one.
+__global__ void __launch_bounds__(256) k_tile_stats(const double *__restrict__ ts, int ns,
+                                                    const double *__restrict__ tt, int nt,
+                                                    double *__restrict__ out) {
+  __shared__ double red[256];
+  const double *tiles[2] = {ts, tt};
+  const int counts[2] = {ns, nt};
+  for (int set = 0; set < 2; ++set) {
+    for (int q = 0; q < 7; ++q) {  // 3 lo (min), 3 hi (max), half-diagonal (max)
+      const bool is_min = q < 3;
+      double v = is_min ? 1e300 : -1e300;
+      if (q == 6) v = 0.0;
+      for (int i = threadIdx.x; i < counts[set]; i += blockDim.x) {
+        const double *c = tiles[set] + 6 * (size_t)i;
+        if (q < 3) v = fmin(v, c[q] - c[3 + q]);
+        else if (q < 6) v = fmax(v, c[q - 3] + c[q]);
+        else v = fmax(v, sqrt(c[3] * c[3] + c[4] * c[4] + c[5] * c[5]));
+      }
+      red[threadIdx.x] = v;
+      __syncthreads();
+      for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+          red[threadIdx.x] = is_min ? fmin(red[threadIdx.x], red[threadIdx.x + w])
+                                    : fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) out[7 * set + q] = red[0];
+      __syncthreads();
+    }
+  }
+}
+
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+struct Carve {
+  unsigned char *base;
+  size_t off = 0;
+  template <typename T>
+  T *take(size_t count) {
+    T *p = reinterpret_cast<T *>(base + off);
+    off = align256(off + count * sizeof(T));
+    return p;
+  }
+};
+
+// Path-length error bound (metres) from the 14 tile statistics: the same
+// model as the planner of the allocating entry points.
+double bound_from_stats(const double *st) {
+  double gap2 = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    const double g = std::max(0.0, std::max(st[d] - st[7 + 3 + d], st[7 + d] - st[3 + d]));
+    gap2 += g * g;
+  }
+  const double gap = sqrt(gap2);
+  if (!(gap > 0.0)) return INFINITY;
+  const double c = (st[6] + st[13]) * (st[6] + st[13]), rho = c / (2.0 * gap), y = c / gap2;
+  return rho * ldexp(1.0, -21) + c / gap * ldexp(1.0, -24) + rho * y * y / 8.0;
+}
+
+bool is_device_pointer(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int transform_noalloc(int device, int sign, double lambda, const double *amp,
+                      const double *phase, const double *u, size_t N, const double *v,
+                      size_t M, double *y, cudaStream_t s) {
+  if (sign != 1 && sign != -1) return fail(HOLO_ERR_INVALID, "sign must be +1 or -1 (got %d)", sign);
+  if (!(lambda > 0.0) || !isfinite(lambda)) return fail(HOLO_ERR_INVALID, "lambda must be finite and > 0");
+  if ((N && (!amp || !phase || !u)) || (M && (!v || !y)))
+    return fail(HOLO_ERR_INVALID, "null input or output array");
+  for (const void *p : {(const void *)amp, (const void *)phase, (const void *)u, (const void *)v,
+                        (const void *)y})
+    if (p && !is_device_pointer(p))
+      return fail(HOLO_ERR_INVALID, "holo_transform_noalloc takes device pointers only");
+  const size_t lim = (size_t)kSortBlock * 4096;
+  if (N > lim || M > lim) return fail(HOLO_ERR_INVALID, "point count above the supported %zu", lim);
+  if (M == 0) return HOLO_OK;
+
+  unsigned char *base = nullptr;
+  HOLO_TRY(noalloc_scratch(device, &base));
+  if (N == 0) {
+    HOLO_CUDA(cudaMemsetAsync(y, 0, M * sizeof(double2), s));
+    HOLO_CUDA(cudaStreamSynchronize(s));
+    return HOLO_OK;
+  }
+
+  // ---- carve the array ----
+  const int n_pad = (int)((N + 1023) / 1024) * 1024;
+  Carve cv{base};
+  int *err = cv.take<int>(16);
+  double *stats = cv.take<double>(16);
+  double *pos_s = cv.take<double>(3 * (size_t)n_pad);
+  int32_t *order_s = cv.take<int32_t>(N);
+  double *pos_t = cv.take<double>(3 * M);
+  int32_t *order_t = cv.take<int32_t>(M);
+  double *tiles_s = cv.take<double>(6 * (N / 256 + 1));
+  double *tiles_t = cv.take<double>(6 * (M / 256 + 1));
+  double2 *ap = cv.take<double2>(n_pad);
+  const size_t shared_off = cv.off;  // sort scratch first, partial sums later
+  const size_t nmax = std::max(N, M);
+  const size_t hist_n = sort_hist_entries((int)nmax);
+  double *bbox = cv.take<double>(6);
+  double *bscr = cv.take<double>(6 * 1024);
+  uint16_t *keys = cv.take<uint16_t>(nmax);
+  uint32_t *hist = cv.take<uint32_t>(hist_n);
+  uint32_t *scan = cv.take<uint32_t>(hist_n + 4096 + 16);
+  const size_t sort_end = cv.off;
+  const size_t partial_min = align256(M * sizeof(double2));  // one split: written to y directly
+  const size_t need = std::max(sort_end, shared_off);
+  if (need > kNoAllocBytes || shared_off + partial_min > kNoAllocBytes)
+    return fail(HOLO_ERR_INVALID,
+                "problem needs %zu bytes of the %zu-byte no-alloc scratch (N=%zu, M=%zu)",
+                std::max(need, shared_off + partial_min), kNoAllocBytes, N, M);
+
+  HOLO_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));  // the error word starts at zero
+  // ---- tile order of both point sets ----
+  HOLO_TRY(launch_bbox(u, (int)N, bbox, bscr, 1024, s));
+  HOLO_TRY(sort_points(u, (int)N, bbox, order_s, keys, hist, scan, s));
+  HOLO_TRY(launch_gather_pos(u, order_s, (int)N, n_pad, pos_s, s));
+  HOLO_TRY(launch_bbox(v, (int)M, bbox, bscr, 1024, s));
+  HOLO_TRY(sort_points(v, (int)M, bbox, order_t, keys, hist, scan, s));
+  HOLO_TRY(launch_gather_pos(v, order_t, (int)M, (int)M, pos_t, s));
+
+  // ---- tile size: the largest whose path-length error bound holds ----
+  const int cands[] = {0, 2, 3, 4};
+  const double budget = 5e-6 * 400e-9 / (2.0 * M_PI);
+  int variant = cands[0];
+  for (int i = 0; i < 4; ++i) {
+    if (M < 4096 && cands[i] == 0) continue;
+    if (M < 1024 && cands[i] == 2) continue;
+    const Variant C = split_variant(cands[i]);
+    const int ns = (int)((N + C.cs - 1) / C.cs), nt = (int)((M + C.tt() - 1) / C.tt());
+    HOLO_TRY(launch_tile_bbox(pos_s, (int)N, C.cs, tiles_s, s));
+    HOLO_TRY(launch_tile_bbox(pos_t, (int)M, C.tt(), tiles_t, s));
+    k_tile_stats<<<1, 256, 0, s>>>(tiles_s, ns, tiles_t, nt, stats);
+    HOLO_CUDA(cudaGetLastError());
+    double st[14];
+    HOLO_CUDA(cudaMemcpyAsync(st, stats, sizeof(st), cudaMemcpyDeviceToHost, s));
+    HOLO_CUDA(cudaStreamSynchronize(s));
+    variant = cands[i];
+    if (bound_from_stats(st) <= budget) break;
+  }
+  const Variant V = split_variant(variant);
+
+  // ---- splits: as many as the occupancy wants and the array holds ----
+  int sm = 0, occ = 0;
+  HOLO_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device));
+  HOLO_TRY(split_occupancy(variant, false, &occ));
+  const int G = std::max(1, occ) * sm;
+  const int n_stiles = (int)((N + V.cs - 1) / V.cs), n_ttiles = (int)((M + V.tt() - 1) / V.tt());
+  const int fit = (int)std::max<size_t>(1, (kNoAllocBytes - shared_off) / (M * sizeof(double2)));
+  int splits = 1;
+  {
+    double best = 1e300;
+    for (int S = 1; S <= std::min(n_stiles, fit); ++S) {
+      const long long waves = ((long long)n_ttiles * S + G - 1) / G;
+      const double cost = waves * (ceil((double)n_stiles / S) + 0.35);
+      if (cost < best * 0.999) {
+        best = cost;
+        splits = S;
+      }
+    }
+  }
+  Carve pc{base, shared_off};
+  double2 *partial = splits > 1 ? pc.take<double2>((size_t)splits * M) : nullptr;
+
+  // ---- gather, pair kernel, split reduction ----
+  HOLO_TRY(launch_gather_ap(amp, phase, order_s, (int)N, n_pad, ap, s));
+  SplitProblem P{};
+  P.pos_s = pos_s;
+  P.ap_s = ap;
+  P.tiles_s = tiles_s;
+  P.pos_t = pos_t;
+  P.tiles_t = tiles_t;
+  P.order_t = order_t;
+  P.partial = partial;
+  P.y = reinterpret_cast<double2 *>(y);
+  P.N = (int)N;
+  P.M = (int)M;
+  P.n_stiles = n_stiles;
+  P.n_ttiles = n_ttiles;
+  P.splits = splits;
+  P.sign = sign;
+  P.sk = sign * ((2.0 * M_PI) / lambda);
+  P.sub = 1;
+  const int grid = std::max(1, std::min(G, n_ttiles * splits));
+  HOLO_TRY(launch_split(P, variant, grid, false, false, err, s));
+  if (splits > 1) HOLO_TRY(launch_reduce(partial, splits, (int)M, order_t, P.y, s));
+  int e = 0;
+  HOLO_CUDA(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HOLO_CUDA(cudaStreamSynchronize(s));
+  if (e) return fail(HOLO_ERR_TIMEOUT, "a device-side wait ran out of time (code %d)", e);
+  return HOLO_OK;
+}
+
+}  // namespace
+}  // namespace holo
+
+extern "C" int holo_transform_noalloc(int device, int sign, double lambda, const double *amp,
+                                      const double *phase, const double *u_xyz, size_t N,
+                                      const double *v_xyz, size_t M, double *y_re_im,
+                                      holo_stream_t stream) {
+  std::lock_guard<std::mutex> lk(holo::g_noalloc_mu);
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) {
+    cudaGetLastError();
+    return holo::fail(HOLO_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return holo::fail(HOLO_ERR_INVALID, "cannot select device %d", device);
+  }
+  const int rc = holo::transform_noalloc(device, sign, lambda, amp, phase, u_xyz, N, v_xyz, M,
+                                         y_re_im, (cudaStream_t)stream);
+  cudaSetDevice(prev);
+  return rc;
+}

@@ -218,6 +218,26 @@ int holo_profile_begin(holo_handle h);
 int holo_profile_end(holo_handle h, double *total_ms, int *launches);
 int holo_probe_peak(holo_handle h, int kind, double *ops_per_s);
 
+/* ---- transform without any device allocation ------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate GPU memory -- hosts that own the whole device memory budget,
+ * plugins running inside another framework's allocator, or real-time loops
+ * that must not hit cudaMalloc/cudaFree and their implicit synchronisation.
+ * Same result as holo_transform(..., HOLO_SPLIT32, ...) on device pointers
+ * (amp, phase, u_xyz, v_xyz, y_re_im must all be device memory; there is no
+ * handle, the device is given by index).  All scratch comes from one fixed
+ * 64 MiB array in the library's device code, held on every GPU that loads the
+ * library until the process exits; problems that do not fit are rejected with
+ * HOLO_ERR_INVALID.  Every call shares that array and overwrites it, so calls
+ * that overlap on the GPU race: calls in one process are serialised by a lock
+ * and each returns only after its work on `stream` has finished.  The first
+ * call on a device looks up the array's address (cudaGetSymbolAddress); make
+ * it before any stream capture. */
+int holo_transform_noalloc(int device, int sign, double lambda, const double *amp,
+                           const double *phase, const double *u_xyz, size_t N,
+                           const double *v_xyz, size_t M, double *y_re_im,
+                           holo_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
