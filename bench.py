@@ -209,6 +209,38 @@ def run_profile_case(args):
         print(json.dumps({"profile_case": pl.info(), "pairs_per_launch": len(amp) * len(vv)}))
 
 
+def run_sweep(args):
+    """One JSON line per split-FP32 variant: pair kernel rate on the config-2 y pass."""
+    import torch
+    import __graft_entry__ as entry
+    entry._load_build_module().build()
+    holo = entry.load_package()
+    amp, phase, u, v, _ = workload()
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+    d = [t(a) for a in (amp, phase, u, v)]
+    h = holo.handle(0)
+    ref = None
+    for var in holo.variants("split32"):
+        try:
+            holo.transform(*d, -1, LAM, precision="split32", variant=var["variant"])
+            torch.cuda.synchronize()
+            h.profile_begin()
+            for _ in range(2):
+                y = holo.transform(*d, -1, LAM, precision="split32", variant=var["variant"])
+            ms, n = h.profile_end()
+        except holo.HoloError as e:
+            print(json.dumps({"variant": var, "error": str(e)}), flush=True)
+            continue
+        yv = y.cpu().numpy()
+        if ref is None:
+            ref = yv
+        rate = 2 * len(amp) * len(v) / (ms * 1e-3)
+        print(json.dumps({"variant": var, "kernel_pairs_per_s": rate, "ms": ms / n,
+                          "rel_l2_vs_first": float(np.linalg.norm(yv - ref) / np.linalg.norm(ref))}),
+              flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -220,11 +252,15 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: two split-FP32 passes of the 512^2 sources onto "
                          "a 256^2 patch of the projector (1.7e10 pairs each), then exit")
+    ap.add_argument("--sweep-variants", action="store_true",
+                    help="time every split-FP32 kernel variant on the config-2 y pass, then exit")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_case:
         return run_profile_case(args)
+    if args.sweep_variants:
+        return run_sweep(args)
 
     import torch
     import torch.distributed as dist

@@ -418,10 +418,12 @@ def variants(precision="split32") -> list[dict]:
     pr = _precision(precision)
     out = []
     for i in range(L.holo_variant_count(pr)):
-        t, r, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        N.check(L.holo_variant_describe(pr, i, ctypes.byref(t), ctypes.byref(r), ctypes.byref(c)))
+        t, r, c, q = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        N.check(L.holo_variant_describe(pr, i, ctypes.byref(t), ctypes.byref(r), ctypes.byref(c),
+                                        ctypes.byref(q)))
         out.append({"variant": i, "threads": t.value, "targets_per_thread": r.value,
-                    "source_tile": c.value, "target_tile": t.value * r.value})
+                    "source_tile": c.value, "target_tile": t.value * r.value,
+                    "fma_sincos_targets": q.value})
     return out
 
 

@@ -963,7 +963,7 @@ int holo_variant_count(int precision) {
 }
 
 int holo_variant_describe(int precision, int variant, int *threads, int *targets_per_thread,
-                          int *source_tile) {
+                          int *source_tile, int *fma_sincos_targets) {
   const int n = holo_variant_count(precision);
   if (n < 0) return n;
   if (variant < 0 || variant >= n) return fail(HOLO_ERR_INVALID, "variant %d out of range", variant);
@@ -971,6 +971,7 @@ int holo_variant_describe(int precision, int variant, int *threads, int *targets
   if (threads) *threads = V.threads;
   if (targets_per_thread) *targets_per_thread = V.r;
   if (source_tile) *source_tile = V.cs;
+  if (fma_sincos_targets) *fma_sincos_targets = V.poly;
   return HOLO_OK;
 }
 

@@ -58,6 +58,7 @@ struct Variant {
   int threads;  // threads per CTA
   int r;        // targets per thread (register blocking)
   int cs;       // sources per tile (one bulk copy per tile)
+  int poly = 0; // targets per thread whose sin/cos run on the FMA pipe
   int tt() const { return threads * r; }
 };
 

@@ -88,6 +88,32 @@ __device__ __forceinline__ void build_frame(Frame *fr, const double *t0, const d
   fr->b0 = reduce_two_pi(sk * r0);
 }
 
+// sin and cos of theta on the FMA pipe: theta -> f = theta / 2 pi - rint(theta / 2 pi)
+// in [-1/2, 1/2] turns, then sin(2 pi f) = f P(f^2) (degree 11) and
+// cos(2 pi f) = Q(f^2) (degree 12), minimax fits made by gen_sincos_poly.py
+// (Lawson's iteration on Chebyshev nodes); float32 Horner error <= 7.6e-7.
+// Used for POLY of the R targets per thread so the XU pipe (MUFU sin/cos,
+// 16 lanes/clk/SM) and the FMA pipe (128 lanes/clk/SM) share the work.
+__device__ __forceinline__ void poly_sincos(float th, float *sn, float *cs) {
+  const float t = th * 0.159154943f;
+  const float n = (t + 12582912.0f) - 12582912.0f;  // round to nearest for |t| < 2^22
+  const float f = t - n;
+  const float f2 = f * f;
+  float s = fmaf(-1.227126217e+01f, f2, 4.120539474e+01f);
+  s = fmaf(s, f2, -7.658010101e+01f);
+  s = fmaf(s, f2, 8.159618378e+01f);
+  s = fmaf(s, f2, -4.134142303e+01f);
+  s = fmaf(s, f2, 6.283182621e+00f);
+  float c = fmaf(6.529610157e+00f, f2, -2.596831322e+01f);
+  c = fmaf(c, f2, 6.016783142e+01f);
+  c = fmaf(c, f2, -8.545016479e+01f);
+  c = fmaf(c, f2, 6.493911743e+01f);
+  c = fmaf(c, f2, -1.973920441e+01f);
+  c = fmaf(c, f2, 1.0f);
+  *sn = s * f;
+  *cs = c;
+}
+
 // One raw (FP64) staging buffer: the bulk copy of tile j+1 is issued once the
 // frame phase of tile j has consumed it, so it overlaps tile j's pair loop.
 template <int THREADS, int R, int CS>
@@ -105,7 +131,7 @@ struct SplitSmem {
 
 // Process one work item: target tile `tt`, source tiles [sb, se), writing into
 // partial slot `split` (or the final output when the problem has one split).
-template <int THREADS, int R, int CS, bool CONST, bool MC>
+template <int THREADS, int R, int CS, int POLY, bool CONST, bool MC>
 __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int split, int sb,
                                              int se, unsigned char *smem, uint32_t &par0,
                                              uint32_t &par1, int *err) {
@@ -275,8 +301,15 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
           const float g = h * ir;
           const float th = fmaf(h, fmaf(g, kap8, kap2), q.w);
           const float w = a * ir;
-          re[r] = fmaf(w, ptx::cos_approx(th), re[r]);
-          im[r] = fmaf(w, ptx::sin_approx(th), im[r]);
+          float sn, cs;
+          if (r < POLY) {
+            poly_sincos(th, &sn, &cs);  // FMA pipe
+          } else {
+            sn = ptx::sin_approx(th);   // XU (MUFU) pipe
+            cs = ptx::cos_approx(th);
+          }
+          re[r] = fmaf(w, cs, re[r]);
+          im[r] = fmaf(w, sn, im[r]);
         }
       }
     }
@@ -316,7 +349,7 @@ __device__ __forceinline__ void split_range(int n, int splits, int s, int *b, in
   *e = (int)(((long long)n * (s + 1)) / splits);
 }
 
-template <int THREADS, int R, int CS, bool CONST, bool MC>
+template <int THREADS, int R, int CS, int POLY, bool CONST, bool MC>
 __global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
     k_split(const SplitProblem P, int n_items, int *err) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -335,12 +368,12 @@ __global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
     const int split = item % P.splits;
     int sb, se;
     split_range(n_src, P.splits, split, &sb, &se);
-    if (!process_item<THREADS, R, CS, CONST, MC>(P, tt, split, sb, se, smem, par0, par1, err))
+    if (!process_item<THREADS, R, CS, POLY, CONST, MC>(P, tt, split, sb, se, smem, par0, par1, err))
       return;
   }
 }
 
-template <int THREADS, int R, int CS>
+template <int THREADS, int R, int CS, int POLY>
 __global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
     k_split_batched(const SplitProblem *__restrict__ probs, const WorkItem *__restrict__ items,
                     int n_items, int *queue, int *err) {
@@ -362,7 +395,7 @@ __global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
     if (it >= n_items) break;
     const WorkItem w = items[it];
     const SplitProblem P = probs[w.problem];
-    if (!process_item<THREADS, R, CS, false, false>(P, w.ttile, w.split, w.s_begin, w.s_end,
+    if (!process_item<THREADS, R, CS, POLY, false, false>(P, w.ttile, w.split, w.s_begin, w.s_end,
                                                     smem, par0, par1, err))
       return;
   }
@@ -370,19 +403,22 @@ __global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
 
 // ---- variant table ------------------------------------------------------------
 constexpr Variant kVariants[] = {
-    {256, 8, 1024}, // 0: TT 2048
-    {128, 8, 1024}, // 1: TT 1024
-    {256, 4, 1024}, // 2: TT 1024
-    {128, 4, 512},  // 3: TT 512
-    {128, 2, 256},  // 4: TT 256 (Monte Carlo blocks of 256 targets)
-    {256, 8, 512},  // 5: TT 2048, short source tiles
+    {256, 8, 1024, 0},  // 0: TT 2048
+    {128, 8, 1024, 0},  // 1: TT 1024
+    {256, 4, 1024, 0},  // 2: TT 1024
+    {128, 4, 512, 0},   // 3: TT 512
+    {128, 2, 256, 0},   // 4: TT 256 (Monte Carlo blocks of 256 targets)
+    {256, 8, 512, 0},   // 5: TT 2048, short source tiles
+    {256, 8, 1024, 1},  // 6: as 0, 1 of 8 targets per thread on the FMA-pipe sin/cos
+    {256, 8, 1024, 2},  // 7: as 0, 2 of 8
+    {256, 8, 1024, 3},  // 8: as 0, 3 of 8
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-template <int THREADS, int R, int CS, bool CONST, bool MC>
+template <int THREADS, int R, int CS, int POLY, bool CONST, bool MC>
 int launch_one(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
   using L = SplitSmem<THREADS, R, CS>;
-  auto kern = k_split<THREADS, R, CS, CONST, MC>;
+  auto kern = k_split<THREADS, R, CS, POLY, CONST, MC>;
   HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)L::bytes));
   const int n_items = p.n_ttiles * p.splits;
@@ -392,20 +428,20 @@ int launch_one(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
   return HOLO_OK;
 }
 
-template <int THREADS, int R, int CS>
+template <int THREADS, int R, int CS, int POLY>
 int launch_variant(const SplitProblem &p, int grid, bool cst, bool mc, int *err,
                    cudaStream_t s) {
-  if (cst && mc) return launch_one<THREADS, R, CS, true, true>(p, grid, err, s);
-  if (cst) return launch_one<THREADS, R, CS, true, false>(p, grid, err, s);
-  if (mc) return launch_one<THREADS, R, CS, false, true>(p, grid, err, s);
-  return launch_one<THREADS, R, CS, false, false>(p, grid, err, s);
+  if (cst && mc) return launch_one<THREADS, R, CS, POLY, true, true>(p, grid, err, s);
+  if (cst) return launch_one<THREADS, R, CS, POLY, true, false>(p, grid, err, s);
+  if (mc) return launch_one<THREADS, R, CS, POLY, false, true>(p, grid, err, s);
+  return launch_one<THREADS, R, CS, POLY, false, false>(p, grid, err, s);
 }
 
-template <int THREADS, int R, int CS>
+template <int THREADS, int R, int CS, int POLY>
 int batched_variant(const SplitProblem *probs, const WorkItem *items, int n_items, int *queue,
                     int grid, int *err, cudaStream_t s) {
   using L = SplitSmem<THREADS, R, CS>;
-  auto kern = k_split_batched<THREADS, R, CS>;
+  auto kern = k_split_batched<THREADS, R, CS, POLY>;
   HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)L::bytes));
   kern<<<grid, THREADS, L::bytes, s>>>(probs, items, n_items, queue, err); note_launches(1);
@@ -413,10 +449,10 @@ int batched_variant(const SplitProblem *probs, const WorkItem *items, int n_item
   return HOLO_OK;
 }
 
-template <int THREADS, int R, int CS>
+template <int THREADS, int R, int CS, int POLY>
 int occupancy_variant(bool mc, int *out) {
   using L = SplitSmem<THREADS, R, CS>;
-  auto kern = mc ? k_split<THREADS, R, CS, false, true> : k_split<THREADS, R, CS, false, false>;
+  auto kern = mc ? k_split<THREADS, R, CS, POLY, false, true> : k_split<THREADS, R, CS, POLY, false, false>;
   HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)L::bytes));
   HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, THREADS, L::bytes));
@@ -430,37 +466,40 @@ Variant split_variant(int i) { return kVariants[i]; }
 
 #define HOLO_SPLIT_DISPATCH(V, CALL)                      \
   switch (V) {                                            \
-    case 0: return CALL(256, 8, 1024);                     \
-    case 1: return CALL(128, 8, 1024);                     \
-    case 2: return CALL(256, 4, 1024);                     \
-    case 3: return CALL(128, 4, 512);                     \
-    case 4: return CALL(128, 2, 256);                     \
-    case 5: return CALL(256, 8, 512);                    \
+    case 0: return CALL(256, 8, 1024, 0);                 \
+    case 1: return CALL(128, 8, 1024, 0);                 \
+    case 2: return CALL(256, 4, 1024, 0);                 \
+    case 3: return CALL(128, 4, 512, 0);                  \
+    case 4: return CALL(128, 2, 256, 0);                  \
+    case 5: return CALL(256, 8, 512, 0);                  \
+    case 6: return CALL(256, 8, 1024, 1);                 \
+    case 7: return CALL(256, 8, 1024, 2);                 \
+    case 8: return CALL(256, 8, 1024, 3);                 \
     default: return fail(HOLO_ERR_INVALID, "unknown split variant %d", V); \
   }
 
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
                  int *err, cudaStream_t s) {
-#define CALL(T, R, C) launch_variant<T, R, C>(p, grid, const_phase, mc, err, s)
+#define CALL(T, R, C, P) launch_variant<T, R, C, P>(p, grid, const_phase, mc, err, s)
   HOLO_SPLIT_DISPATCH(variant, CALL)
 #undef CALL
 }
 
 int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,
                          int *queue, int variant, int grid, int *err, cudaStream_t s) {
-#define CALL(T, R, C) batched_variant<T, R, C>(probs_dev, items, n_items, queue, grid, err, s)
+#define CALL(T, R, C, P) batched_variant<T, R, C, P>(probs_dev, items, n_items, queue, grid, err, s)
   HOLO_SPLIT_DISPATCH(variant, CALL)
 #undef CALL
 }
 
 int split_occupancy(int variant, bool mc, int *ctas_per_sm) {
-#define CALL(T, R, C) occupancy_variant<T, R, C>(mc, ctas_per_sm)
+#define CALL(T, R, C, P) occupancy_variant<T, R, C, P>(mc, ctas_per_sm)
   HOLO_SPLIT_DISPATCH(variant, CALL)
 #undef CALL
 }
 
 int split_smem_bytes(int variant) {
-#define CALL(T, R, C) (int)SplitSmem<T, R, C>::bytes
+#define CALL(T, R, C, P) (int)SplitSmem<T, R, C>::bytes
   HOLO_SPLIT_DISPATCH(variant, CALL)
 #undef CALL
 }

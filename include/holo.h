@@ -198,7 +198,7 @@ int holo_transform_batched(holo_handle h, const holo_problem *problems, int n_pr
  * The Python layer persists the table as JSON. */
 int holo_variant_count(int precision);
 int holo_variant_describe(int precision, int variant, int *threads, int *targets_per_thread,
-                          int *source_tile);
+                          int *source_tile, int *fma_sincos_targets);
 int holo_set_variant(holo_handle h, int precision, int bucket, int variant);
 int holo_get_variant(holo_handle h, int precision, int bucket, int *variant);
 int holo_size_bucket(size_t N, size_t M);
