@@ -121,8 +121,8 @@ struct SplitSmem {
   static constexpr size_t raw_pos = 0;                                   // double [CS*3]
   static constexpr size_t raw_ap = raw_pos + CS * 3 * sizeof(double);    // double2 [CS]
   static constexpr size_t rec = raw_ap + CS * sizeof(double2);           // float4 [CS]
-  static constexpr size_t amp = rec + CS * sizeof(float4);                // float [CS]
-  static constexpr size_t acc = (amp + CS * sizeof(float) + 15) / 16 * 16;  // double2 [R][THREADS]
+  static constexpr size_t amp = rec + CS * sizeof(float4);                // float2 [CS]
+  static constexpr size_t acc = (amp + CS * sizeof(float2) + 15) / 16 * 16;  // double2 [R][THREADS]
   static constexpr size_t bphase = acc + R * THREADS * sizeof(double2);      // float [R][THREADS]
   static constexpr size_t frame = (bphase + R * THREADS * sizeof(float) + 15) / 16 * 16;
   static constexpr size_t bar = frame + sizeof(Frame);                    // uint64 [2]
@@ -140,7 +140,7 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
   double *raw_pos = reinterpret_cast<double *>(smem + L::raw_pos);
   double2 *raw_ap = reinterpret_cast<double2 *>(smem + L::raw_ap);
   float4 *rec = reinterpret_cast<float4 *>(smem + L::rec);
-  float *ramp = reinterpret_cast<float *>(smem + L::amp);
+  float2 *ramp = reinterpret_cast<float2 *>(smem + L::amp);
   Frame *fr = reinterpret_cast<Frame *>(smem + L::frame);
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::bar);
   // FP64 carries and the per-target phase B live in shared memory (index
@@ -150,7 +150,6 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
   const int tid = threadIdx.x;
   const double sk = P.sk;
   const float kap2 = (float)(0.5 * sk);    // s k / 2
-  const float kap8 = (float)(0.125 * sk);  // s k / 8
   const int n_strata = MC ? (P.N + P.sub - 1) / P.sub : 0;
 
   auto issue = [&](int j) {
@@ -230,28 +229,29 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
           if (CONST) am = (double)size;
         }
       }
+      // record: (-2 Sx, -2 Sy, Ps, A) and (a, Sx^2 + Sy^2), so that per pair
+      // c = |d_perp|^2 = (T2 + S2) - 2 (Tx Sx + Ty Sy) costs one add and two FMAs
       float4 q;
-      float a;
+      float2 a;
       if (valid) {
         const double dx = sx - fr->s0[0], dy = sy - fr->s0[1], dz = sz - fr->s0[2];
         const double ps = fma(e0, dx, fma(e1_, dy, e2_ * dz));
         const double A = CONST ? 0.0 : reduce_two_pi(fma(-sk, ps, ph));
         const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-        q.x = fmaf(f1x, fx, fmaf(f1y, fy, f1z * fz));
-        q.y = fmaf(f2x, fx, fmaf(f2y, fy, f2z * fz));
-        q.z = (float)ps;
-        q.w = (float)A;
-        a = CONST ? (MC ? (float)am : 1.0f) : (float)am;
+        const float Sx = fmaf(f1x, fx, fmaf(f1y, fy, f1z * fz));
+        const float Sy = fmaf(f2x, fx, fmaf(f2y, fy, f2z * fz));
+        q = make_float4(-2.f * Sx, -2.f * Sy, (float)ps, (float)A);
+        a = make_float2(CONST ? (MC ? (float)am : 1.0f) : (float)am, fmaf(Sx, Sx, Sy * Sy));
       } else {
         q = make_float4(0.f, 0.f, -1e18f, 0.f);  // r ~ 1e18: contributes 0
-        a = 0.f;
+        a = make_float2(0.f, 0.f);
       }
       rec[i] = q;
       ramp[i] = a;
     }
 
     // ---- per-thread target frame ----
-    float Tx[R], Ty[R], Qt[R];
+    float Tx[R], Ty[R], Qt[R], T2[R], kq[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int ti = tt * TT + tid + r * THREADS;
@@ -267,7 +267,12 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       const float fx = (float)tx, fy = (float)ty, fz = (float)tz;
       Tx[r] = fmaf(f1x, fx, fmaf(f1y, fy, f1z * fz));
       Ty[r] = fmaf(f2x, fx, fmaf(f2y, fy, f2z * fz));
-      Qt[r] = (float)(fr->r0 + pt);
+      const double qt = fr->r0 + pt;
+      Qt[r] = (float)qt;
+      T2[r] = fmaf(Tx[r], Tx[r], Ty[r] * Ty[r]);
+      // curvature correction s k c^2 / (8 r^3) = h * c * (s k / 8) / r^2 with
+      // 1/r^2 taken as 1/Qt^2 (relative error ~2 |Ps| / r0 of a ~1e-6 rad term)
+      kq[r] = (float)(0.125 * sk / (qt * qt));
       bph[r * THREADS + tid] = (float)B;
     }
     __syncthreads();
@@ -284,23 +289,20 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
 #pragma unroll 2
     for (int s = 0; s < count; ++s) {
       const float4 q = rec[s];
-      const float a = ramp[s];
+      const float2 as = ramp[s];
       if (CONST) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) re[r] += a;
+        for (int r = 0; r < R; ++r) re[r] += as.x;
       } else {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          const float dx = Tx[r] - q.x;
-          const float dy = Ty[r] - q.y;
-          const float c = fmaf(dy, dy, dx * dx);
+          const float c = fmaf(Tx[r], q.x, fmaf(Ty[r], q.y, T2[r] + as.y));
           const float qq = Qt[r] - q.z;
           const float r2 = fmaf(qq, qq, c);
           const float ir = ptx::rsqrt_approx(r2);
           const float h = c * ir;
-          const float g = h * ir;
-          const float th = fmaf(h, fmaf(g, kap8, kap2), q.w);
-          const float w = a * ir;
+          const float th = fmaf(h, fmaf(c, kq[r], kap2), q.w);
+          const float w = as.x * ir;
           float sn, cs;
           if (r < POLY) {
             poly_sincos(th, &sn, &cs);  // FMA pipe
@@ -412,6 +414,8 @@ constexpr Variant kVariants[] = {
     {256, 8, 1024, 1},  // 6: as 0, 1 of 8 targets per thread on the FMA-pipe sin/cos
     {256, 8, 1024, 2},  // 7: as 0, 2 of 8
     {256, 8, 1024, 3},  // 8: as 0, 3 of 8
+    {256, 4, 1024, 1},  // 9: as 2, 1 of 4
+    {256, 8, 1024, 4},  // 10: as 0, 4 of 8
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -475,6 +479,8 @@ Variant split_variant(int i) { return kVariants[i]; }
     case 6: return CALL(256, 8, 1024, 1);                 \
     case 7: return CALL(256, 8, 1024, 2);                 \
     case 8: return CALL(256, 8, 1024, 3);                 \
+    case 9: return CALL(256, 4, 1024, 1);                 \
+    case 10: return CALL(256, 8, 1024, 4);                \
     default: return fail(HOLO_ERR_INVALID, "unknown split variant %d", V); \
   }
 
