@@ -119,8 +119,8 @@ struct Scratch {
 
 int default_split_variant(size_t N, size_t M) {
   (void)N;
-  if (M >= 4096) return 0;
-  if (M >= 1024) return 2;
+  if (M >= 4096) return 7;  // 256 x 8 targets, 1024-source tiles, 2 of 8 on FMA sin/cos
+  if (M >= 1024) return 9;
   return 3;
 }
 
@@ -294,7 +294,7 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
     // path-length error bound holds (sparse or wide point sets need small tiles)
     std::vector<int> cands = {variant};
     if (forced_variant < 0)
-      for (int c : {0, 2, 3, 4})
+      for (int c : {7, 9, 3, 4})
         if (split_variant(c).tt() < split_variant(variant).tt() ||
             (split_variant(c).tt() == split_variant(variant).tt() &&
              split_variant(c).cs < split_variant(variant).cs))

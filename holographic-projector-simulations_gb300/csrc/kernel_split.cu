@@ -272,7 +272,7 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       T2[r] = fmaf(Tx[r], Tx[r], Ty[r] * Ty[r]);
       // curvature correction s k c^2 / (8 r^3) = h * c * (s k / 8) / r^2 with
       // 1/r^2 taken as 1/Qt^2 (relative error ~2 |Ps| / r0 of a ~1e-6 rad term)
-      kq[r] = (float)(0.125 * sk / (qt * qt));
+      kq[r] = __fdividef(0.25f * kap2, Qt[r] * Qt[r]);
       bph[r * THREADS + tid] = (float)B;
     }
     __syncthreads();
