@@ -326,7 +326,14 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
   p->splits = choose_splits(p->n_ttiles, p->n_stiles, G, M, max_splits);
   p->grid = std::max(1, std::min(G, p->n_ttiles * p->splits));
 
-  if (precision != HOLO_SPLIT32) {
+  if (precision == HOLO_SPLIT32) {
+    // float-float offsets of every point from its tile's centre (tiles of the
+    // chosen variant, whose boxes the last bound evaluation left in tiles_s/t)
+    HOLO_TRY(alloc_plan(p.get(), (void **)&p->geo_s, (size_t)6 * p->n_pad * sizeof(float), s));
+    HOLO_TRY(alloc_plan(p.get(), (void **)&p->geo_t, (size_t)6 * std::max<size_t>(M, 1) * sizeof(float), s));
+    HOLO_TRY(launch_rel_hilo(p->pos_s, (int)N, p->n_pad, p->tiles_s, V.cs, p->geo_s, s));
+    HOLO_TRY(launch_rel_hilo(p->pos_t, (int)M, (int)M, p->tiles_t, V.tt(), p->geo_t, s));
+  } else {
     HOLO_TRY(alloc_plan(p.get(), (void **)&p->pos_s, (size_t)3 * p->n_pad * sizeof(double), s));
     HOLO_TRY(alloc_plan(p.get(), (void **)&p->pos_t, (size_t)3 * std::max<size_t>(M, 1) * sizeof(double), s));
     HOLO_TRY(launch_pack_pos(u, (int)N, p->n_pad, p->pos_s, s));
@@ -361,10 +368,14 @@ int plan_execute_impl(holo_plan_s *p, int sign, double lambda, const double *amp
   const double k = (2.0 * M_PI) / lambda;
   const bool cst = (flags & HOLO_FLAG_CONST_PHASE) != 0;
   if (p->precision == HOLO_SPLIT32) {
-    HOLO_TRY(launch_gather_ap(amp, phase, p->order_s, p->N, p->n_pad, ap, s));
+    float2 *apf = reinterpret_cast<float2 *>(ap);  // n_pad float pairs fit in the buffer
+    HOLO_TRY(launch_gather_apf(amp, phase, p->order_s, p->N, p->n_pad, apf, s));
     SplitProblem P{};
+    P.geo_s = p->geo_s;
+    P.apf_s = apf;
+    P.geo_t = p->geo_t;
     P.pos_s = p->pos_s;
-    P.ap_s = ap;
+    P.ap_s = nullptr;
     P.tiles_s = p->tiles_s;
     P.pos_t = p->pos_t;
     P.tiles_t = p->tiles_t;
@@ -445,17 +456,22 @@ static int plan_execute_mc_impl(holo_plan_s *p, int sign, double lambda, const d
   if (!ap || (splits > 1 && !partial)) return fail(HOLO_ERR_ALLOC, "execute scratch");
   // tile boxes for the Monte Carlo block size when the plan was tiled differently
   const double *tiles_s = p->tiles_s, *tiles_t = p->tiles_t;
+  const float *geo_t = p->geo_t;
   if (v != p->variant) {
     double *ts = tmp.get<double>((size_t)6 * n_stiles);
     double *tt = tmp.get<double>((size_t)6 * n_ttiles);
-    if (!ts || !tt) return fail(HOLO_ERR_ALLOC, "execute scratch");
+    float *gt = tmp.get<float>((size_t)6 * p->M);
+    if (!ts || !tt || !gt) return fail(HOLO_ERR_ALLOC, "execute scratch");
     HOLO_TRY(launch_tile_bbox(p->pos_s, p->N, V.cs, ts, s));
     HOLO_TRY(launch_tile_bbox(p->pos_t, p->M, V.tt(), tt, s));
+    HOLO_TRY(launch_rel_hilo(p->pos_t, p->M, p->M, tt, V.tt(), gt, s));
     tiles_s = ts;
     tiles_t = tt;
+    geo_t = gt;
   }
   HOLO_TRY(launch_gather_ap(amp, phase, p->order_s, p->N, p->n_pad, ap, s));
   SplitProblem P{};
+  P.geo_t = geo_t;
   P.pos_s = p->pos_s;
   P.ap_s = ap;
   P.tiles_s = tiles_s;

@@ -35,7 +35,7 @@ int batch_build(holo_batch_s *b, const holo_problem *pr, int n, int precision, c
   BatchState st;
   // FP64 batches are captured as a sequence of per-problem launches.
   const bool split = precision == HOLO_SPLIT32;
-  st.variant = 0;
+  st.variant = 7;  // the default variant for large target sets
   const Variant V = split ? split_variant(st.variant) : fp64_variant(0);
   int occ = 1;
   if (split) HOLO_TRY(split_occupancy(st.variant, false, &occ));
@@ -65,6 +65,8 @@ int batch_build(holo_batch_s *b, const holo_problem *pr, int n, int precision, c
     SplitProblem &P = st.probs[i];
     P = SplitProblem{};
     P.pos_s = p->pos_s;
+    P.geo_s = p->geo_s;
+    P.geo_t = p->geo_t;
     P.tiles_s = p->tiles_s;
     P.pos_t = p->pos_t;
     P.tiles_t = p->tiles_t;
@@ -81,7 +83,7 @@ int batch_build(holo_batch_s *b, const holo_problem *pr, int n, int precision, c
     double2 *ap = (double2 *)pool_alloc(h, (size_t)p->n_pad * sizeof(double2), s);
     if (!ap) return fail(HOLO_ERR_ALLOC, "batch gather buffer");
     b->owned.push_back(ap);
-    P.ap_s = ap;
+    P.apf_s = reinterpret_cast<float2 *>(ap);
     if (splits > 1) {
       double2 *part = (double2 *)pool_alloc(h, (size_t)splits * p->M * sizeof(double2), s);
       if (!part) return fail(HOLO_ERR_ALLOC, "batch partial buffer");
@@ -138,8 +140,8 @@ int batch_build(holo_batch_s *b, const holo_problem *pr, int n, int precision, c
     return cuda_fail(e, "cudaStreamBeginCapture", __FILE__, __LINE__);
   }
   for (int i = 0; i < n && rc == HOLO_OK; ++i)
-    rc = launch_gather_ap(pr[i].amp, pr[i].phase, b->plans[i]->order_s, b->plans[i]->N,
-                          b->plans[i]->n_pad, (double2 *)st.probs[i].ap_s, cap);
+    rc = launch_gather_apf(pr[i].amp, pr[i].phase, b->plans[i]->order_s, b->plans[i]->N,
+                          b->plans[i]->n_pad, const_cast<float2 *>(st.probs[i].apf_s), cap);
   if (rc == HOLO_OK && cudaMemsetAsync(st.queue, 0, sizeof(int), cap) != cudaSuccess)
     rc = fail(HOLO_ERR_CUDA, "queue reset during capture");
   if (rc == HOLO_OK && st.n_items > 0)

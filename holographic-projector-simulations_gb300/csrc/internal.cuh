@@ -69,8 +69,12 @@ Variant fp64_variant(int i);
 
 // ---- device-side problem descriptor (one plan execute) ------------------------
 struct SplitProblem {
-  const double *pos_s;     // sources, tile order, absolute xyz (3 * Ns_pad)
-  const double2 *ap_s;     // sources, tile order, (phase, amp)   (Ns_pad)
+  const float *geo_s;      // sources, tile order: offset from own tile centre, float-float
+                           // (hi xyz, lo xyz) x Ns_pad
+  const float2 *apf_s;     // sources, tile order, (phase mod 2 pi, amp) floats (Ns_pad)
+  const float *geo_t;      // targets, tile order: offset from own tile centre, float-float (M)
+  const double *pos_s;     // sources, tile order, absolute xyz (3 * Ns_pad); Monte Carlo
+  const double2 *ap_s;     // sources, tile order, (phase, amp) (Ns_pad); Monte Carlo
   const double *tiles_s;   // source tiles of `cs` points: centre xyz, half xyz
   const double *pos_t;     // targets, tile order, absolute xyz (3 * M)
   const double *tiles_t;   // target tiles of `tt` points
@@ -122,6 +126,10 @@ int launch_pack_ap(const double *amp, const double *phase, int n, int n_pad, dou
                    cudaStream_t s);
 int launch_pack_pos(const double *pos, int n, int n_pad, double *out, cudaStream_t s);
 int launch_iota(int32_t *order, int n, cudaStream_t s);
+int launch_rel_hilo(const double *pos_sorted, int n, int n_out, const double *tiles, int tile,
+                    float *out, cudaStream_t s);
+int launch_gather_apf(const double *amp, const double *phase, const int32_t *order, int n,
+                      int n_pad, float2 *out, cudaStream_t s);
 
 // kernel_split.cu
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
@@ -187,6 +195,8 @@ struct holo_plan_s {
   double *tiles_t = nullptr;     // 6 * n_ttiles
   int32_t *order_s = nullptr;    // N (split only)
   int32_t *order_t = nullptr;    // M (split only)
+  float *geo_s = nullptr;        // split: float-float offsets from the tile centres
+  float *geo_t = nullptr;
   double *u_orig = nullptr;      // original-order positions (for the adjoint)
   double *v_orig = nullptr;
   std::vector<void *> owned;     // everything allocated for the plan

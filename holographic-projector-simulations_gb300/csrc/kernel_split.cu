@@ -33,7 +33,45 @@ struct __align__(16) Frame {
   double s0[3];  // source tile centre
   float ef[3], e1[3], e2[3];
   float r0f;
+  float ah[3], al[3];  // s k e as float-float (hi + lo)
+  float b0h, b0l;      // b0 as float-float
 };
+
+// ---- float-float (double-single) helpers: error-free transformations --------
+// (Knuth's TwoSum; the product error by FMA).  The _rn intrinsics keep the
+// compiler from fusing or reassociating the steps that must round alone.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// S + E ~ (ah + al) . (th + tl) over 3 components, relative error ~2^-44.
+__device__ __forceinline__ void dot3_ff(const float *ah, const float *al, const float *th,
+                                        const float *tl, float &S, float &E) {
+  float p[3], e[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    p[d] = __fmul_rn(ah[d], th[d]);
+    e[d] = fmaf(ah[d], th[d], -p[d]);
+    e[d] = fmaf(ah[d], tl[d], e[d]);
+    e[d] = fmaf(al[d], th[d], e[d]);
+  }
+  float s1, t1, t2;
+  two_sum(p[0], p[1], s1, t1);
+  two_sum(s1, p[2], S, t2);
+  E = __fadd_rn(__fadd_rn(t1, t2), __fadd_rn(__fadd_rn(e[0], e[1]), e[2]));
+}
+
+// (S + E) reduced mod 2 pi to about [-pi, pi] in float, |S| < 2^16: three-part
+// Cody-Waite with C1 = 6.28125 (8 significant bits, so n C1 and S - n C1 are exact).
+__device__ __forceinline__ float reduce_two_pi_ff(float S, float E) {
+  const float n = __fsub_rn(__fadd_rn(__fmul_rn(S, 0.159154943f), 12582912.0f), 12582912.0f);
+  float r = fmaf(-n, 6.28125f, S);
+  r = fmaf(-n, 1.935307169e-3f, r);   // fl32(2 pi - C1)
+  r = fmaf(-n, 1.025313168e-11f, r);  // fl32(2 pi - C1 - C2)
+  return __fadd_rn(r, E);
+}
 
 // Philox4x32-10 (Salmon et al., SC'11); same rounds as the oracle.
 __device__ __forceinline__ uint32_t philox_first(uint32_t c0, uint32_t c1, uint32_t k0,
@@ -86,6 +124,13 @@ __device__ __forceinline__ void build_frame(Frame *fr, const double *t0, const d
   fr->r0 = r0;
   fr->r0f = (float)r0;
   fr->b0 = reduce_two_pi(sk * r0);
+  for (int d = 0; d < 3; ++d) {
+    const double a = sk * e[d];
+    fr->ah[d] = (float)a;
+    fr->al[d] = (float)(a - (double)fr->ah[d]);
+  }
+  fr->b0h = (float)fr->b0;
+  fr->b0l = (float)(fr->b0 - (double)fr->b0h);
 }
 
 // sin and cos of theta on the FMA pipe: theta -> f = theta / 2 pi - rint(theta / 2 pi)
@@ -114,13 +159,14 @@ __device__ __forceinline__ void poly_sincos(float th, float *sn, float *cs) {
   *cs = c;
 }
 
-// One raw (FP64) staging buffer: the bulk copy of tile j+1 is issued once the
-// frame phase of tile j has consumed it, so it overlaps tile j's pair loop.
+// One staging buffer of source records (float-float offsets + (phase, amp)):
+// the bulk copy of tile j+1 is issued once the frame phase of tile j has
+// consumed it, so it overlaps tile j's pair loop.
 template <int THREADS, int R, int CS>
 struct SplitSmem {
-  static constexpr size_t raw_pos = 0;                                   // double [CS*3]
-  static constexpr size_t raw_ap = raw_pos + CS * 3 * sizeof(double);    // double2 [CS]
-  static constexpr size_t rec = raw_ap + CS * sizeof(double2);           // float4 [CS]
+  static constexpr size_t raw_geo = 0;                                   // float [CS*6]
+  static constexpr size_t raw_apf = raw_geo + CS * 6 * sizeof(float);    // float2 [CS]
+  static constexpr size_t rec = raw_apf + CS * sizeof(float2);           // float4 [CS]
   static constexpr size_t amp = rec + CS * sizeof(float4);                // float2 [CS]
   static constexpr size_t acc = (amp + CS * sizeof(float2) + 15) / 16 * 16;  // double2 [R][THREADS]
   static constexpr size_t bphase = acc + R * THREADS * sizeof(double2);      // float [R][THREADS]
@@ -137,8 +183,8 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
                                              uint32_t &par1, int *err) {
   using L = SplitSmem<THREADS, R, CS>;
   constexpr int TT = THREADS * R;
-  double *raw_pos = reinterpret_cast<double *>(smem + L::raw_pos);
-  double2 *raw_ap = reinterpret_cast<double2 *>(smem + L::raw_ap);
+  float *raw_geo = reinterpret_cast<float *>(smem + L::raw_geo);
+  float2 *raw_apf = reinterpret_cast<float2 *>(smem + L::raw_apf);
   float4 *rec = reinterpret_cast<float4 *>(smem + L::rec);
   float2 *ramp = reinterpret_cast<float2 *>(smem + L::amp);
   Frame *fr = reinterpret_cast<Frame *>(smem + L::frame);
@@ -153,10 +199,10 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
   const int n_strata = MC ? (P.N + P.sub - 1) / P.sub : 0;
 
   auto issue = [&](int j) {
-    // tile j of CS sources: CS*24 B of positions + CS*16 B of (phase, amp)
-    ptx::mbar_arrive_expect_tx(&bar[0], CS * (3 * sizeof(double) + sizeof(double2)));
-    ptx::bulk_g2s(raw_pos, P.pos_s + (size_t)j * CS * 3, CS * 3 * sizeof(double), &bar[0]);
-    ptx::bulk_g2s(raw_ap, P.ap_s + (size_t)j * CS, CS * sizeof(double2), &bar[0]);
+    // tile j of CS sources: CS*24 B of float-float offsets + CS*8 B of (phase, amp)
+    ptx::mbar_arrive_expect_tx(&bar[0], CS * (6 * sizeof(float) + sizeof(float2)));
+    ptx::bulk_g2s(raw_geo, P.geo_s + (size_t)j * CS * 6, CS * 6 * sizeof(float), &bar[0]);
+    ptx::bulk_g2s(raw_apf, P.apf_s + (size_t)j * CS, CS * sizeof(float2), &bar[0]);
   };
   (void)par1;
 
@@ -199,23 +245,40 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       __syncthreads();
     }
 
-    // ---- phase A: per-source records of this tile pair ----
-    const double e0 = fr->e[0], e1_ = fr->e[1], e2_ = fr->e[2];
+    // ---- phase A: per-source records of this tile pair (FP32 pipe) ----
+    // A = phi - s k e.s' needs ~1e-7 rad of ~1e3 rad: float-float products of
+    // (s k e) and the offset s' (precomputed per plan), then a float reduction.
     const float f1x = fr->e1[0], f1y = fr->e1[1], f1z = fr->e1[2];
     const float f2x = fr->e2[0], f2y = fr->e2[1], f2z = fr->e2[2];
+    const float fex = fr->ef[0], fey = fr->ef[1], fez = fr->ef[2];
+    float ah[3], al[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      ah[d] = fr->ah[d];
+      al[d] = fr->al[d];
+    }
     for (int i = tid; i < CS; i += THREADS) {
       bool valid;
-      double sx, sy, sz, ph, am;
+      float sh[3], A, am;
       if (!MC) {
         valid = j * CS + i < P.N;
-        const double *sp = raw_pos + 3 * i;
-        const double2 a2 = raw_ap[i];
-        sx = sp[0]; sy = sp[1]; sz = sp[2];
-        ph = a2.x; am = a2.y;
+        const float *g = raw_geo + 6 * i;
+        const float sl[3] = {g[3], g[4], g[5]};
+        sh[0] = g[0]; sh[1] = g[1]; sh[2] = g[2];
+        const float2 pa = raw_apf[i];
+        float S, E;
+        dot3_ff(ah, al, sh, sl, S, E);
+        float S2, E2;
+        two_sum(pa.x, -S, S2, E2);
+        A = CONST ? 0.f : reduce_two_pi_ff(S2, __fsub_rn(E2, E));
+        am = CONST ? 1.f : pa.y;
       } else {
+        // Monte Carlo: sampled sources from anywhere in the chunk's strata, FP64
         const int st = j * CS + i;
         valid = st < n_strata;
-        sx = sy = sz = ph = am = 0.0;
+        sh[0] = sh[1] = sh[2] = 0.f;
+        A = 0.f;
+        am = 0.f;
         if (valid) {
           const int start = st * P.sub;
           const int size = min(P.sub, P.N - start);
@@ -223,10 +286,11 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
           const int sidx = start + (int)(rnd % (uint32_t)size);
           const double *sp = P.pos_s + 3 * (size_t)sidx;
           const double2 a2 = P.ap_s[sidx];
-          sx = sp[0]; sy = sp[1]; sz = sp[2];
-          ph = a2.x;
-          am = a2.y * (double)size;
-          if (CONST) am = (double)size;
+          const double dx = sp[0] - fr->s0[0], dy = sp[1] - fr->s0[1], dz = sp[2] - fr->s0[2];
+          const double ps = fma(fr->e[0], dx, fma(fr->e[1], dy, fr->e[2] * dz));
+          A = CONST ? 0.f : (float)reduce_two_pi(fma(-sk, ps, a2.x));
+          sh[0] = (float)dx; sh[1] = (float)dy; sh[2] = (float)dz;
+          am = CONST ? (float)size : (float)(a2.y * (double)size);
         }
       }
       // record: (-2 Sx, -2 Sy, Ps, A) and (a, Sx^2 + Sy^2), so that per pair
@@ -234,14 +298,11 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       float4 q;
       float2 a;
       if (valid) {
-        const double dx = sx - fr->s0[0], dy = sy - fr->s0[1], dz = sz - fr->s0[2];
-        const double ps = fma(e0, dx, fma(e1_, dy, e2_ * dz));
-        const double A = CONST ? 0.0 : reduce_two_pi(fma(-sk, ps, ph));
-        const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-        const float Sx = fmaf(f1x, fx, fmaf(f1y, fy, f1z * fz));
-        const float Sy = fmaf(f2x, fx, fmaf(f2y, fy, f2z * fz));
-        q = make_float4(-2.f * Sx, -2.f * Sy, (float)ps, (float)A);
-        a = make_float2(CONST ? (MC ? (float)am : 1.0f) : (float)am, fmaf(Sx, Sx, Sy * Sy));
+        const float Sx = fmaf(f1x, sh[0], fmaf(f1y, sh[1], f1z * sh[2]));
+        const float Sy = fmaf(f2x, sh[0], fmaf(f2y, sh[1], f2z * sh[2]));
+        const float Ps = fmaf(fex, sh[0], fmaf(fey, sh[1], fez * sh[2]));
+        q = make_float4(-2.f * Sx, -2.f * Sy, Ps, A);
+        a = make_float2(am, fmaf(Sx, Sx, Sy * Sy));
       } else {
         q = make_float4(0.f, 0.f, -1e18f, 0.f);  // r ~ 1e18: contributes 0
         a = make_float2(0.f, 0.f);
@@ -250,30 +311,31 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       ramp[i] = a;
     }
 
-    // ---- per-thread target frame ----
+    // ---- per-thread target frame (FP32 pipe, float-float for B) ----
     float Tx[R], Ty[R], Qt[R], T2[R], kq[R];
+    const float r0f = fr->r0f, b0h = fr->b0h, b0l = fr->b0l;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int ti = tt * TT + tid + r * THREADS;
-      double tx = 0.0, ty = 0.0, tz = 0.0;
+      float th[3] = {0.f, 0.f, 0.f}, tl[3] = {0.f, 0.f, 0.f};
       if (ti < P.M) {
-        const double *tp = P.pos_t + 3 * (size_t)ti;
-        tx = tp[0] - fr->t0[0];
-        ty = tp[1] - fr->t0[1];
-        tz = tp[2] - fr->t0[2];
+        const float *g = P.geo_t + 6 * (size_t)ti;
+        th[0] = g[0]; th[1] = g[1]; th[2] = g[2];
+        tl[0] = g[3]; tl[1] = g[4]; tl[2] = g[5];
       }
-      const double pt = fma(e0, tx, fma(e1_, ty, e2_ * tz));
-      const double B = reduce_two_pi(fma(sk, pt, fr->b0));
-      const float fx = (float)tx, fy = (float)ty, fz = (float)tz;
-      Tx[r] = fmaf(f1x, fx, fmaf(f1y, fy, f1z * fz));
-      Ty[r] = fmaf(f2x, fx, fmaf(f2y, fy, f2z * fz));
-      const double qt = fr->r0 + pt;
-      Qt[r] = (float)qt;
+      // B = s k (r0 + e.t') mod 2 pi
+      float S, E, S2, E2;
+      dot3_ff(ah, al, th, tl, S, E);
+      two_sum(S, b0h, S2, E2);
+      const float B = reduce_two_pi_ff(S2, __fadd_rn(__fadd_rn(E, E2), b0l));
+      Tx[r] = fmaf(f1x, th[0], fmaf(f1y, th[1], f1z * th[2]));
+      Ty[r] = fmaf(f2x, th[0], fmaf(f2y, th[1], f2z * th[2]));
+      Qt[r] = r0f + fmaf(fex, th[0], fmaf(fey, th[1], fez * th[2]));
       T2[r] = fmaf(Tx[r], Tx[r], Ty[r] * Ty[r]);
       // curvature correction s k c^2 / (8 r^3) = h * c * (s k / 8) / r^2 with
       // 1/r^2 taken as 1/Qt^2 (relative error ~2 |Ps| / r0 of a ~1e-6 rad term)
       kq[r] = __fdividef(0.25f * kap2, Qt[r] * Qt[r]);
-      bph[r * THREADS + tid] = (float)B;
+      bph[r * THREADS + tid] = B;
     }
     __syncthreads();
     // the staging buffer is free: fetch the next tile while this one is summed

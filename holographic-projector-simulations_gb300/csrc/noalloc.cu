@@ -161,6 +161,8 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
   double *tiles_s = cv.take<double>(6 * (N / 256 + 1));
   double *tiles_t = cv.take<double>(6 * (M / 256 + 1));
   double2 *ap = cv.take<double2>(n_pad);
+  float *geo_s = cv.take<float>(6 * (size_t)n_pad);
+  float *geo_t = cv.take<float>(6 * M);
   const size_t shared_off = cv.off;  // sort scratch first, partial sums later
   const size_t nmax = std::max(N, M);
   const size_t hist_n = sort_hist_entries((int)nmax);
@@ -206,6 +208,9 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
     if (bound_from_stats(st) <= budget) break;
   }
   const Variant V = split_variant(variant);
+  // the last bound evaluation left this variant's tile boxes in tiles_s / tiles_t
+  HOLO_TRY(launch_rel_hilo(pos_s, (int)N, n_pad, tiles_s, V.cs, geo_s, s));
+  HOLO_TRY(launch_rel_hilo(pos_t, (int)M, (int)M, tiles_t, V.tt(), geo_t, s));
 
   // ---- splits: as many as the occupancy wants and the array holds ----
   int sm = 0, occ = 0;
@@ -230,10 +235,13 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
   double2 *partial = splits > 1 ? pc.take<double2>((size_t)splits * M) : nullptr;
 
   // ---- gather, pair kernel, split reduction ----
-  HOLO_TRY(launch_gather_ap(amp, phase, order_s, (int)N, n_pad, ap, s));
+  float2 *apf = reinterpret_cast<float2 *>(ap);
+  HOLO_TRY(launch_gather_apf(amp, phase, order_s, (int)N, n_pad, apf, s));
   SplitProblem P{};
+  P.geo_s = geo_s;
+  P.apf_s = apf;
+  P.geo_t = geo_t;
   P.pos_s = pos_s;
-  P.ap_s = ap;
   P.tiles_s = tiles_s;
   P.pos_t = pos_t;
   P.tiles_t = tiles_t;

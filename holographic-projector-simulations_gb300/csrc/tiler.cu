@@ -278,6 +278,46 @@ __global__ void __launch_bounds__(256) k_gather_ap(const double *__restrict__ am
   }
 }
 
+// Offsets of tile-ordered points from their tile's centre as float-float pairs:
+// out[6 i .. 6 i + 2] = hi = fl32(p - c), out[6 i + 3 .. 6 i + 5] = lo =
+// fl32((p - c) - hi); zeros for the padding i >= n.
+__global__ void __launch_bounds__(256) k_rel_hilo(const double *__restrict__ pos, int n,
+                                                  int n_out, const double *__restrict__ tiles,
+                                                  int tile, float *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += gridDim.x * blockDim.x) {
+    float *o = out + 6 * (size_t)i;
+    if (i < n) {
+      const double *c = tiles + 6 * (size_t)(i / tile);
+      for (int d = 0; d < 3; ++d) {
+        const double r = pos[3 * (size_t)i + d] - c[d];
+        const float hi = (float)r;
+        o[d] = hi;
+        o[3 + d] = (float)(r - (double)hi);
+      }
+    } else {
+      for (int d = 0; d < 6; ++d) o[d] = 0.f;
+    }
+  }
+}
+
+// (phase reduced to [-pi, pi], amplitude) in float, tile order.
+__global__ void __launch_bounds__(256) k_gather_apf(const double *__restrict__ amp,
+                                                    const double *__restrict__ phase,
+                                                    const int32_t *__restrict__ order, int n,
+                                                    int n_pad, float2 *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += gridDim.x * blockDim.x) {
+    if (i < n) {
+      const int j = order ? order[i] : i;
+      const double p = phase[j];
+      const double q = rint(p * kInvTwoPi);  // two-constant Cody-Waite reduction
+      const double r = fma(-q, kTwoPiLo, fma(-q, kTwoPiHi, p));
+      out[i] = make_float2((float)r, (float)amp[j]);
+    } else {
+      out[i] = make_float2(0.f, 0.f);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) k_iota(int32_t *__restrict__ order, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     order[i] = i;
@@ -354,6 +394,22 @@ int launch_gather_ap(const double *amp, const double *phase, const int32_t *orde
 int launch_pack_ap(const double *amp, const double *phase, int n, int n_pad, double2 *out,
                    cudaStream_t s) {
   return launch_gather_ap(amp, phase, nullptr, n, n_pad, out, s);
+}
+
+int launch_rel_hilo(const double *pos_sorted, int n, int n_out, const double *tiles, int tile,
+                    float *out, cudaStream_t s) {
+  if (n_out <= 0) return HOLO_OK;
+  k_rel_hilo<<<grid_for(n_out, 256, 8192), 256, 0, s>>>(pos_sorted, n, n_out, tiles, tile, out); note_launches(1);
+  HOLO_CUDA(cudaGetLastError());
+  return HOLO_OK;
+}
+
+int launch_gather_apf(const double *amp, const double *phase, const int32_t *order, int n,
+                      int n_pad, float2 *out, cudaStream_t s) {
+  if (n_pad <= 0) return HOLO_OK;
+  k_gather_apf<<<grid_for(n_pad, 256, 8192), 256, 0, s>>>(amp, phase, order, n, n_pad, out); note_launches(1);
+  HOLO_CUDA(cudaGetLastError());
+  return HOLO_OK;
 }
 
 int launch_iota(int32_t *order, int n, cudaStream_t s) {
