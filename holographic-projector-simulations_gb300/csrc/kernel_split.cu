@@ -13,12 +13,16 @@
 //   rho = c / (q + r) = (c / 2r) (1 + c / (4 r^2) + O(c^2 / r^4)),
 //   s k r = [phi-independent] s k (r0 + e.t')  - s k e.s'  + s k rho.
 // The two linear terms are separable and large (k |t'| ~ 1e3 rad): they are
-// evaluated in FP64 once per target (B) and once per source (A) per tile pair
-// and reduced mod 2 pi (two-constant Cody-Waite).  Per pair only the small
+// evaluated once per target (B) and once per source (A) per tile pair, in
+// float-float arithmetic on the FP32 pipe from offsets the plan precomputes as
+// hi/lo float pairs, and reduced mod 2 pi (three-part Cody-Waite); only the
+// frame itself (one thread per tile pair) is FP64.  Per pair only the small
 // curvature term s k rho (|rho| / r0 ~ 1e-6) and the amplitude 1/r are formed
 // in FP32; their sensitivity to FP32 rounding of d is suppressed by |d| / r0.
-// Per pair: 14 FP32 ops + 3 MUFU ops (rsqrt, sin, cos).  Sums run in FP32
-// over one source tile (CS terms), are rotated by e^{iB} and carried in FP64.
+// Per pair: 12 FP32 ops + 3 MUFU ops (rsqrt, sin, cos); POLY of the R targets
+// per thread take sin/cos from an FMA-pipe polynomial instead (17 FP32 ops,
+// 1 MUFU).  Sums run in FP32 over one source tile (CS terms), are rotated by
+// e^{iB} and carried in FP64.
 #include "internal.cuh"
 #include "ptx.cuh"
 
@@ -173,6 +177,17 @@ struct SplitSmem {
   static constexpr size_t frame = (bphase + R * THREADS * sizeof(float) + 15) / 16 * 16;
   static constexpr size_t bar = frame + sizeof(Frame);                    // uint64 [2]
   static constexpr size_t bytes = bar + 2 * sizeof(uint64_t);
+};
+
+// CTAs per SM the launch bounds ask for: as many as shared memory holds (228 KB
+// per SM, 1 KB reserved per CTA), at most what 128 (R >= 8) or 80 (R < 8)
+// registers per thread allow.
+template <int THREADS, int R, int CS>
+struct SplitMinBlocks {
+  static constexpr int by_smem = (int)(233472 / (SplitSmem<THREADS, R, CS>::bytes + 1024));
+  static constexpr int by_regs = 65536 / (THREADS * (R >= 8 ? 128 : 80));
+  static constexpr int m = by_smem < by_regs ? by_smem : by_regs;
+  static constexpr int value = m < 1 ? 1 : (m > 8 ? 8 : m);
 };
 
 // Process one work item: target tile `tt`, source tiles [sb, se), writing into
@@ -414,7 +429,7 @@ __device__ __forceinline__ void split_range(int n, int splits, int s, int *b, in
 }
 
 template <int THREADS, int R, int CS, int POLY, bool CONST, bool MC>
-__global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
+__global__ void __launch_bounds__(THREADS, SplitMinBlocks<THREADS, R, CS>::value)
     k_split(const SplitProblem P, int n_items, int *err) {
   extern __shared__ __align__(128) unsigned char smem[];
   using L = SplitSmem<THREADS, R, CS>;
@@ -438,7 +453,7 @@ __global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
 }
 
 template <int THREADS, int R, int CS, int POLY>
-__global__ void __launch_bounds__(THREADS, 256 / THREADS * 2)
+__global__ void __launch_bounds__(THREADS, SplitMinBlocks<THREADS, R, CS>::value)
     k_split_batched(const SplitProblem *__restrict__ probs, const WorkItem *__restrict__ items,
                     int n_items, int *queue, int *err) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -478,6 +493,8 @@ constexpr Variant kVariants[] = {
     {256, 8, 1024, 3},  // 8: as 0, 3 of 8
     {256, 4, 1024, 1},  // 9: as 2, 1 of 4
     {256, 8, 1024, 4},  // 10: as 0, 4 of 8
+    {256, 4, 512, 1},   // 11: 3 CTAs/SM
+    {128, 4, 512, 1},   // 12: 5 CTAs/SM
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -543,6 +560,8 @@ Variant split_variant(int i) { return kVariants[i]; }
     case 8: return CALL(256, 8, 1024, 3);                 \
     case 9: return CALL(256, 4, 1024, 1);                 \
     case 10: return CALL(256, 8, 1024, 4);                \
+    case 11: return CALL(256, 4, 512, 1);                 \
+    case 12: return CALL(128, 4, 512, 1);                 \
     default: return fail(HOLO_ERR_INVALID, "unknown split variant %d", V); \
   }
 
