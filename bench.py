@@ -32,9 +32,15 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 LAM = 632.8e-9
 METRIC = "pair-evals/s split-FP32 vs FP64 on 1 GB300 at rel-L2≤1e-5; % FP32/SFU peak"
-MUFU_PER_PAIR = 3    # rsqrt, sin, cos
-FP32_PER_PAIR = 14   # FP32 pipe instructions per pair in the inner loop
 FLOP_PER_PAIR = 29   # the reference's FLOP_PER_POINT (cuda/macros.h:71-80)
+
+
+def pipe_ops_per_pair(variant: dict) -> tuple[float, float]:
+    """(MUFU ops, FP32-pipe ops) per pair of a split-kernel variant: 3 MUFU (rsqrt,
+    sin, cos) + 12 FP32 per pair, except that `fma_sincos_targets` of every
+    `targets_per_thread` take sin/cos from the FMA-pipe polynomial (+16 FP32, -2 MUFU)."""
+    f = variant["fma_sincos_targets"] / variant["targets_per_thread"]
+    return 3.0 - 2.0 * f, 12.0 + 16.0 * f
 WORKLOAD = "config2: 512^2 sources -> 1024^2 projector -> 512^2 projection (x->y->z)"
 
 
@@ -209,6 +215,113 @@ def run_profile_case(args):
         print(json.dumps({"profile_case": pl.info(), "pairs_per_launch": len(amp) * len(vv)}))
 
 
+def _events_ms(fn, reps=1):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        out = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps, out
+
+
+def run_other_workload(args):
+    """Configs 1, 3, 4, 5: one JSON line each (not the headline line)."""
+    import torch
+    import __graft_entry__ as entry
+    entry._load_build_module().build()
+    holo = entry.load_package()
+    from holo_gb300 import torch_ops
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+    rng = np.random.default_rng(0)
+
+    def grid_t(n, pitch, z):
+        return grid(n, pitch, z)
+
+    out = {"workload": args.workload, "data": "synthetic (seeded)"}
+    if args.workload in ("config1", "config3"):
+        u = grid(64, 10e-6, 0.35)
+        v = grid(256, 7.56e-6, 0.0)
+        amp = rng.uniform(0, 1, len(u))
+        phase = rng.uniform(0, 2 * np.pi, len(u))
+        d = [t(a) for a in (amp, phase, u, v, u)]
+        if args.workload == "config1":
+            for prec in ("fp64", "split32"):
+                holo.project(*d, LAM, precision=prec)
+                ms, _ = _events_ms(lambda: holo.project(*d, LAM, precision=prec), reps=3)
+                out[prec] = {"ms_per_chain": ms,
+                             "pair_evals_per_s": 2 * len(u) * len(v) / (ms * 1e-3)}
+            out["pairs_per_chain"] = 2 * len(u) * len(v)
+        else:
+            y64 = holo.transform(*d[:4], -1, LAM, precision="fp64").cpu().numpy()
+            holo.transform_mc(*d[:4], -1, LAM, seed=1, subsample=16, targets_per_block=256)
+            ms, ymc = _events_ms(lambda: holo.transform_mc(*d[:4], -1, LAM, seed=2,
+                                                           subsample=16, targets_per_block=256),
+                                 reps=3)
+            ymc = ymc.cpu().numpy()
+            ms_bf, _ = _events_ms(lambda: holo.transform(*d[:4], -1, LAM, precision="split32"),
+                                  reps=3)
+            out.update({
+                "mc_ms": ms, "brute_force_split32_ms": ms_bf,
+                "sampled_pair_evals_per_s": len(u) // 16 * len(v) / (ms * 1e-3),
+                "effective_pair_evals_per_s": len(u) * len(v) / (ms * 1e-3),
+                "mc_rel_l2_vs_fp64": float(np.linalg.norm(ymc - y64) / np.linalg.norm(y64)),
+                "config": "x->y pass of config 1, 1/16 of the sources per block of 256 targets"})
+    elif args.workload == "config4":
+        probs, pairs = [], 0
+        for i in range(64):
+            ns = int(np.exp(rng.uniform(np.log(1024), np.log(262144))))
+            side = int(np.ceil(np.sqrt(ns)))
+            u = grid(side, 10e-6, rng.uniform(0.2, 0.5))[:ns]
+            ms_side = int(rng.choice([128, 256, 512, 1024]))
+            v = grid(ms_side, 7.56e-6, 0.0)
+            amp, phase = rng.uniform(0, 1, ns), rng.uniform(0, 2 * np.pi, ns)
+            y = torch.zeros(2 * len(v), dtype=torch.float64, device=dev)
+            probs.append(holo.Problem(t(amp), t(phase), t(u), t(v), -1, LAM, y))
+            pairs += ns * len(v)
+        with holo.Batch(probs, "split32") as b:
+            b.execute()
+            ms_b, _ = _events_ms(b.execute, reps=3)
+        plans = [holo.Plan(p.u, p.v, "split32") for p in probs]
+        for pl, p in zip(plans, probs):
+            pl.execute(p.amp, p.phase, -1, LAM)
+        ms_s, _ = _events_ms(lambda: [pl.execute(p.amp, p.phase, -1, LAM)
+                                      for pl, p in zip(plans, probs)], reps=2)
+        for pl in plans:
+            pl.close()
+        out.update({"problems": 64, "pairs": pairs, "batched_ms": ms_b, "sequential_ms": ms_s,
+                    "batched_pair_evals_per_s": pairs / (ms_b * 1e-3),
+                    "sequential_pair_evals_per_s": pairs / (ms_s * 1e-3),
+                    "speedup": ms_s / ms_b,
+                    "config": "N log-uniform [1024, 262144], M in {128^2..1024^2}, z0 U[0.2,0.5]"})
+    else:  # config5
+        pp = t(grid(1024, 7.56e-6, 0.0)).reshape(-1, 3)
+        tp = t(grid(512, 10e-6, 0.35)).reshape(-1, 3)
+        n = 512
+        yy, xx = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+        img = np.zeros((n, n))
+        for _ in range(8):
+            cx, cy = rng.uniform(0, n, 2)
+            img += rng.uniform(0.2, 1) * np.exp(-((xx - cx) ** 2 + (yy - cy) ** 2) /
+                                                 (2 * rng.uniform(5, 40) ** 2))
+        target = t((img / img.mean()).ravel())
+        steps = args.steps if args.steps != 5 else 100
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, losses = torch_ops.optimise_phase_hologram(pp, tp, target, LAM, steps=steps, lr=0.05)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        pairs_step = 2 * pp.shape[0] * tp.shape[0]
+        out.update({"adam_steps": steps, "seconds": dt, "s_per_step": dt / steps,
+                    "pair_evals_per_s": pairs_step * steps / dt, "loss_first": losses[0],
+                    "loss_last": losses[-1],
+                    "config": "1024^2 phases -> 512^2 target intensity, forward + adjoint per step"})
+    print(json.dumps(out), flush=True)
+
+
 def run_sweep(args):
     """One JSON line per split-FP32 variant: pair kernel rate on the config-2 y pass."""
     import torch
@@ -254,6 +367,10 @@ def main():
                          "a 256^2 patch of the projector (1.7e10 pairs each), then exit")
     ap.add_argument("--sweep-variants", action="store_true",
                     help="time every split-FP32 kernel variant on the config-2 y pass, then exit")
+    ap.add_argument("--workload", default="config2",
+                    choices=["config2", "config1", "config3", "config4", "config5"],
+                    help="config2 (default) is the headline line; the others print their own "
+                         "JSON line: 1 FP64 chain, 3 Monte Carlo, 4 batched, 5 Adam hologram")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -261,6 +378,8 @@ def main():
         return run_profile_case(args)
     if args.sweep_variants:
         return run_sweep(args)
+    if args.workload != "config2":
+        return run_other_workload(args)
 
     import torch
     import torch.distributed as dist
@@ -338,6 +457,11 @@ def main():
     kern_pairs_s = pairs_step * args.steps / (kern_ms * 1e-3) if kern_ms > 0 else 0.0
     mufu_peak = h.probe_peak(0)
     ffma_peak = h.probe_peak(1)
+    with holo.Plan(d_u, d_v, args.precision) as pl:
+        info = pl.info()
+    var = next(x for x in holo.variants(args.precision) if x["variant"] == info["variant"]) \
+        if args.precision == "split32" else None
+    MUFU_PER_PAIR, FP32_PER_PAIR = pipe_ops_per_pair(var) if var else (0.0, 0.0)
     achieved = kern_pairs_s * MUFU_PER_PAIR
     traffic = None
     prof = os.path.join(REPO, "profiles", "split_kernel_traffic.json")
@@ -346,13 +470,18 @@ def main():
             traffic = json.load(open(prof)).get("bytes_per_launch_config2")
         except (OSError, ValueError):
             traffic = None
+    # the pair rate this variant could reach if its busiest pipe ran at the measured peak
+    bound_rate = min(mufu_peak / MUFU_PER_PAIR, ffma_peak / FP32_PER_PAIR) if var else None
     roofline = {"bound": "xu", "achieved": achieved / 1e9, "peak": mufu_peak / 1e9,
                 "unit": "Gop/s", "frac": achieved / mufu_peak if mufu_peak else None,
                 "traffic": traffic,
-                "note": "compute-bound: MUFU (rsqrt, sin, cos = 3 per pair) issue rate of the "
-                        "pair kernel vs the MUFU rate measured by holo_probe_peak; neither HBM "
-                        "nor tensor cores bound this path",
+                "note": "compute-bound: MUFU (XU pipe) ops of the pair kernel per second vs the "
+                        "MUFU rate measured by holo_probe_peak (sin.approx throughput); neither "
+                        "HBM nor tensor cores bound this path",
+                "variant": var, "mufu_per_pair": MUFU_PER_PAIR, "fp32_per_pair": FP32_PER_PAIR,
                 "fp32_frac": kern_pairs_s * FP32_PER_PAIR / ffma_peak if ffma_peak else None,
+                "fma_peak_gops": ffma_peak / 1e9,
+                "pairs_per_s_frac_of_pipe_bound": kern_pairs_s / bound_rate if bound_rate else None,
                 "kernel_pairs_per_s": kern_pairs_s,
                 "kernel_ms_per_launch": kern_ms / max(kern_launches, 1),
                 "kernel_launches": kern_launches}

@@ -119,7 +119,8 @@ struct Scratch {
 
 int default_split_variant(size_t N, size_t M) {
   (void)N;
-  if (M >= 4096) return 7;  // 256 x 8 targets, 1024-source tiles, 2 of 8 on FMA sin/cos
+  // measured on GB300 (config-2 y pass): 256 x 4 targets, 1024-source tiles,
+  // 1 of 4 targets per thread on the FMA-pipe sin/cos is fastest
   if (M >= 1024) return 9;
   return 3;
 }
@@ -294,7 +295,7 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
     // path-length error bound holds (sparse or wide point sets need small tiles)
     std::vector<int> cands = {variant};
     if (forced_variant < 0)
-      for (int c : {7, 9, 3, 4})
+      for (int c : {9, 11, 3, 4})
         if (split_variant(c).tt() < split_variant(variant).tt() ||
             (split_variant(c).tt() == split_variant(variant).tt() &&
              split_variant(c).cs < split_variant(variant).cs))

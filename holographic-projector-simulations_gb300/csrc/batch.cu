@@ -35,7 +35,7 @@ int batch_build(holo_batch_s *b, const holo_problem *pr, int n, int precision, c
   BatchState st;
   // FP64 batches are captured as a sequence of per-problem launches.
   const bool split = precision == HOLO_SPLIT32;
-  st.variant = 7;  // the default variant for large target sets
+  st.variant = 9;  // the default variant for target sets of 1024 and more
   const Variant V = split ? split_variant(st.variant) : fp64_variant(0);
   int occ = 1;
   if (split) HOLO_TRY(split_occupancy(st.variant, false, &occ));

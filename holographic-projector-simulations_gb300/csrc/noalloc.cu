@@ -189,12 +189,11 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
   HOLO_TRY(launch_gather_pos(v, order_t, (int)M, (int)M, pos_t, s));
 
   // ---- tile size: the largest whose path-length error bound holds ----
-  const int cands[] = {7, 9, 3, 4};
+  const int cands[] = {9, 11, 3, 4};
   const double budget = 5e-6 * 400e-9 / (2.0 * M_PI);
   int variant = cands[0];
   for (int i = 0; i < 4; ++i) {
-    if (M < 4096 && cands[i] == 7) continue;
-    if (M < 1024 && cands[i] == 9) continue;
+    if (M < 1024 && (cands[i] == 9 || cands[i] == 11)) continue;
     const Variant C = split_variant(cands[i]);
     const int ns = (int)((N + C.cs - 1) / C.cs), nt = (int)((M + C.tt() - 1) / C.tt());
     HOLO_TRY(launch_tile_bbox(pos_s, (int)N, C.cs, tiles_s, s));
