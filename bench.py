@@ -204,7 +204,9 @@ def run_profile_case(args):
     holo = entry.load_package()
     amp, phase, u, v, _ = workload()
     side = 1024
-    vv = v.reshape(side, side, 3)[384:640, 384:640].reshape(-1, 3)  # central 256^2 patch
+    # central 256^2 patch (split32) or 64^2 patch (fp64, ~0.1 s per launch)
+    lo, hi = (384, 640) if args.precision == "split32" else (480, 544)
+    vv = v.reshape(side, side, 3)[lo:hi, lo:hi].reshape(-1, 3)
     dev = torch.device("cuda", 0)
     t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
     args_ = (t(amp), t(phase), t(u), t(vv))
