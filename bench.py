@@ -37,10 +37,12 @@ FLOP_PER_PAIR = 29   # the reference's FLOP_PER_POINT (cuda/macros.h:71-80)
 
 def pipe_ops_per_pair(variant: dict) -> tuple[float, float]:
     """(MUFU ops, FP32-pipe ops) per pair of a split-kernel variant: 3 MUFU (rsqrt,
-    sin, cos) + 12 FP32 per pair, except that `fma_sincos_targets` of every
-    `targets_per_thread` take sin/cos from the FMA-pipe polynomial (+16 FP32, -2 MUFU)."""
+    sin, cos) + 12 FP32 per pair (10 without the curvature correction), except that
+    `fma_sincos_targets` of every `targets_per_thread` take sin/cos from the
+    FMA-pipe polynomial (+16 FP32, -2 MUFU)."""
     f = variant["fma_sincos_targets"] / variant["targets_per_thread"]
-    return 3.0 - 2.0 * f, 12.0 + 16.0 * f
+    base = 12.0 if variant.get("curvature_term", 1) else 10.0
+    return 3.0 - 2.0 * f, base + 16.0 * f
 WORKLOAD = "config2: 512^2 sources -> 1024^2 projector -> 512^2 projection (x->y->z)"
 
 

@@ -418,12 +418,12 @@ def variants(precision="split32") -> list[dict]:
     pr = _precision(precision)
     out = []
     for i in range(L.holo_variant_count(pr)):
-        t, r, c, q = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        t, r, c, q, k = (ctypes.c_int() for _ in range(5))
         N.check(L.holo_variant_describe(pr, i, ctypes.byref(t), ctypes.byref(r), ctypes.byref(c),
-                                        ctypes.byref(q)))
+                                        ctypes.byref(q), ctypes.byref(k)))
         out.append({"variant": i, "threads": t.value, "targets_per_thread": r.value,
                     "source_tile": c.value, "target_tile": t.value * r.value,
-                    "fma_sincos_targets": q.value})
+                    "fma_sincos_targets": q.value, "curvature_term": k.value})
     return out
 
 

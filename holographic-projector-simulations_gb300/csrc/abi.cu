@@ -222,7 +222,8 @@ static int sort_set(holo_plan_s *p, const double *pos, int n, int n_pad, double 
 //   the two point sets' boxes, rho = c / 2r the FP32 curvature term:
 //   FP32 rounding of rho (~4 ulp), of the in-tile offsets (c / r * 2^-24) and
 //   the truncated series term rho (c / r^2)^2 / 8.
-static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, cudaStream_t s) {
+static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, double *curv,
+                            cudaStream_t s) {
   const int ns = (p->N + cs - 1) / cs, nt = (p->M + tt - 1) / tt;
   HOLO_TRY(launch_tile_bbox(p->pos_s, p->N, cs, p->tiles_s, s));
   HOLO_TRY(launch_tile_bbox(p->pos_t, p->M, tt, p->tiles_t, s));
@@ -255,11 +256,25 @@ static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, cudaS
   const double gap = sqrt(gap2);
   if (!(gap > 0.0) || ns == 0 || nt == 0) {
     *bound = ns && nt ? INFINITY : 0.0;
+    *curv = *bound;
     return HOLO_OK;
   }
   const double c = (hs + ht) * (hs + ht), rho = c / (2.0 * gap), y = c / gap2;
   *bound = rho * ldexp(1.0, -21) + c / gap * ldexp(1.0, -24) + rho * y * y / 8.0;
+  *curv = rho * y / 4.0;  // the curvature term c^2 / 8r^3 a variant may drop
   return HOLO_OK;
+}
+
+// The variant with the same tiles that drops the curvature term (or -1).
+static int no_correction_twin(int v) {
+  const Variant A = split_variant(v);
+  if (!A.corr) return -1;
+  for (int i = 0; i < split_variant_count(); ++i) {
+    const Variant B = split_variant(i);
+    if (!B.corr && B.threads == A.threads && B.r == A.r && B.cs == A.cs && B.poly == A.poly)
+      return i;
+  }
+  return -1;
 }
 
 // Path-length error budget of the split path: 5e-6 rad at lambda = 400 nm.
@@ -302,11 +317,19 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
           cands.push_back(c);
     for (size_t i = 0; i < cands.size(); ++i) {
       const Variant C = split_variant(cands[i]);
-      double bound = 0.0;
-      HOLO_TRY(tile_error_bound(p.get(), C.cs, C.tt(), &bound, s));
+      double bound = 0.0, curv = 0.0;
+      HOLO_TRY(tile_error_bound(p.get(), C.cs, C.tt(), &bound, &curv, s));
       variant = cands[i];
-      p->err_bound = bound;
-      if (bound <= kSplitBoundMetres) break;
+      p->err_bound = C.corr ? bound : bound + curv;
+      if (C.corr && forced_variant < 0) {
+        // the same tiles without the per-pair curvature term, when it is negligible
+        const int twin = no_correction_twin(cands[i]);
+        if (twin >= 0 && bound + curv <= kSplitBoundMetres) {
+          variant = twin;
+          p->err_bound = bound + curv;
+        }
+      }
+      if (p->err_bound <= kSplitBoundMetres) break;
     }
   }
   const Variant V = precision == HOLO_SPLIT32 ? split_variant(variant) : fp64_variant(variant);
@@ -980,7 +1003,7 @@ int holo_variant_count(int precision) {
 }
 
 int holo_variant_describe(int precision, int variant, int *threads, int *targets_per_thread,
-                          int *source_tile, int *fma_sincos_targets) {
+                          int *source_tile, int *fma_sincos_targets, int *curvature_term) {
   const int n = holo_variant_count(precision);
   if (n < 0) return n;
   if (variant < 0 || variant >= n) return fail(HOLO_ERR_INVALID, "variant %d out of range", variant);
@@ -989,6 +1012,7 @@ int holo_variant_describe(int precision, int variant, int *threads, int *targets
   if (targets_per_thread) *targets_per_thread = V.r;
   if (source_tile) *source_tile = V.cs;
   if (fma_sincos_targets) *fma_sincos_targets = V.poly;
+  if (curvature_term) *curvature_term = V.corr;
   return HOLO_OK;
 }
 

@@ -59,6 +59,8 @@ struct Variant {
   int r;        // targets per thread (register blocking)
   int cs;       // sources per tile (one bulk copy per tile)
   int poly = 0; // targets per thread whose sin/cos run on the FMA pipe
+  int corr = 1; // 1: per-pair curvature correction c^2 / 8r^3; 0: dropped (the
+                // planner picks such a variant only when its error bound allows)
   int tt() const { return threads * r; }
 };
 

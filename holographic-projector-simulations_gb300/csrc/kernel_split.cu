@@ -212,6 +212,16 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
   const double sk = P.sk;
   const float kap2 = (float)(0.5 * sk);    // s k / 2
   const int n_strata = MC ? (P.N + P.sub - 1) / P.sub : 0;
+  // POLY = (targets per thread on the FMA-pipe sin/cos) | 16 * (no curvature
+  // correction).  Without the correction the curvature quantities are stored
+  // scaled: c_s = kap2^2 c, q_s = |kap2| q, so r2_s = q_s^2 + c_s = kap2^2 r^2 and
+  // the phase is one FMA, theta' = c_s rsqrt(r2_s) + sign A, where theta =
+  // sign theta' (the sign flips the imaginary part at the end) and the
+  // amplitude a |kap2| absorbs the 1 / |kap2| of rsqrt(r2_s).
+  constexpr int NPOLY = POLY & 15;
+  constexpr bool CORR = (POLY & 16) == 0;
+  const float ak = fabsf(kap2), ak2 = kap2 * kap2;
+  const float sgn = kap2 < 0.f ? -1.f : 1.f;
 
   auto issue = [&](int j) {
     // tile j of CS sources: CS*24 B of float-float offsets + CS*8 B of (phase, amp)
@@ -316,8 +326,13 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
         const float Sx = fmaf(f1x, sh[0], fmaf(f1y, sh[1], f1z * sh[2]));
         const float Sy = fmaf(f2x, sh[0], fmaf(f2y, sh[1], f2z * sh[2]));
         const float Ps = fmaf(fex, sh[0], fmaf(fey, sh[1], fez * sh[2]));
-        q = make_float4(-2.f * Sx, -2.f * Sy, Ps, A);
-        a = make_float2(am, fmaf(Sx, Sx, Sy * Sy));
+        if (CORR || CONST) {
+          q = make_float4(-2.f * Sx, -2.f * Sy, Ps, A);
+          a = make_float2(am, fmaf(Sx, Sx, Sy * Sy));
+        } else {
+          q = make_float4(-2.f * ak2 * Sx, -2.f * ak2 * Sy, ak * Ps, sgn * A);
+          a = make_float2(am * ak, ak2 * fmaf(Sx, Sx, Sy * Sy));
+        }
       } else {
         q = make_float4(0.f, 0.f, -1e18f, 0.f);  // r ~ 1e18: contributes 0
         a = make_float2(0.f, 0.f);
@@ -350,6 +365,10 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       // curvature correction s k c^2 / (8 r^3) = h * c * (s k / 8) / r^2 with
       // 1/r^2 taken as 1/Qt^2 (relative error ~2 |Ps| / r0 of a ~1e-6 rad term)
       kq[r] = __fdividef(0.25f * kap2, Qt[r] * Qt[r]);
+      if (!CORR && !CONST) {
+        Qt[r] *= ak;
+        T2[r] *= ak2;
+      }
       bph[r * THREADS + tid] = B;
     }
     __syncthreads();
@@ -377,11 +396,16 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
           const float qq = Qt[r] - q.z;
           const float r2 = fmaf(qq, qq, c);
           const float ir = ptx::rsqrt_approx(r2);
-          const float h = c * ir;
-          const float th = fmaf(h, fmaf(c, kq[r], kap2), q.w);
+          float th;
+          if (CORR) {
+            const float h = c * ir;
+            th = fmaf(h, fmaf(c, kq[r], kap2), q.w);
+          } else {
+            th = fmaf(c, ir, q.w);  // scaled: sign * theta
+          }
           const float w = as.x * ir;
           float sn, cs;
-          if (r < POLY) {
+          if (r < NPOLY) {
             poly_sincos(th, &sn, &cs);  // FMA pipe
           } else {
             sn = ptx::sin_approx(th);   // XU (MUFU) pipe
@@ -401,8 +425,9 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       } else {
         float sb, cb;
         __sincosf(bph[r * THREADS + tid], &sb, &cb);
-        a.x += (double)fmaf(re[r], cb, -im[r] * sb);
-        a.y += (double)fmaf(re[r], sb, im[r] * cb);
+        const float imr = CORR ? im[r] : sgn * im[r];
+        a.x += (double)fmaf(re[r], cb, -imr * sb);
+        a.y += (double)fmaf(re[r], sb, imr * cb);
       }
       acc[r * THREADS + tid] = a;
     }
@@ -495,6 +520,11 @@ constexpr Variant kVariants[] = {
     {256, 8, 1024, 4},  // 10: as 0, 4 of 8
     {256, 4, 512, 1},   // 11: 3 CTAs/SM
     {128, 4, 512, 1},   // 12: 5 CTAs/SM
+    // without the curvature correction (10 FP32 ops + 3 MUFU per pair)
+    {256, 4, 1024, 1, 0},  // 13: as 9
+    {256, 8, 1024, 2, 0},  // 14: as 7
+    {256, 8, 1024, 3, 0},  // 15: as 8
+    {256, 4, 512, 1, 0},   // 16: as 11
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -562,6 +592,10 @@ Variant split_variant(int i) { return kVariants[i]; }
     case 10: return CALL(256, 8, 1024, 4);                \
     case 11: return CALL(256, 4, 512, 1);                 \
     case 12: return CALL(128, 4, 512, 1);                 \
+    case 13: return CALL(256, 4, 1024, 1 | 16);           \
+    case 14: return CALL(256, 8, 1024, 2 | 16);           \
+    case 15: return CALL(256, 8, 1024, 3 | 16);           \
+    case 16: return CALL(256, 4, 512, 1 | 16);            \
     default: return fail(HOLO_ERR_INVALID, "unknown split variant %d", V); \
   }
 

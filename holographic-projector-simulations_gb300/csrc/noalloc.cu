@@ -103,18 +103,35 @@ struct Carve {
   }
 };
 
-// Path-length error bound (metres) from the 14 tile statistics: the same
-// model as the planner of the allocating entry points.
-double bound_from_stats(const double *st) {
+// Path-length error bound (metres) from the 14 tile statistics, and the
+// curvature term c^2 / 8r^3 a variant may drop: the same model as the planner
+// of the allocating entry points.
+double bound_from_stats(const double *st, double *curv) {
   double gap2 = 0.0;
   for (int d = 0; d < 3; ++d) {
     const double g = std::max(0.0, std::max(st[d] - st[7 + 3 + d], st[7 + d] - st[3 + d]));
     gap2 += g * g;
   }
   const double gap = sqrt(gap2);
-  if (!(gap > 0.0)) return INFINITY;
+  if (!(gap > 0.0)) {
+    *curv = INFINITY;
+    return INFINITY;
+  }
   const double c = (st[6] + st[13]) * (st[6] + st[13]), rho = c / (2.0 * gap), y = c / gap2;
+  *curv = rho * y / 4.0;
   return rho * ldexp(1.0, -21) + c / gap * ldexp(1.0, -24) + rho * y * y / 8.0;
+}
+
+// The variant with the same tiles that drops the curvature term (or -1).
+int no_correction_twin(int v) {
+  const Variant A = split_variant(v);
+  for (int i = 0; i < split_variant_count(); ++i) {
+    const Variant B = split_variant(i);
+    if (A.corr && !B.corr && B.threads == A.threads && B.r == A.r && B.cs == A.cs &&
+        B.poly == A.poly)
+      return i;
+  }
+  return -1;
 }
 
 bool is_device_pointer(const void *p) {
@@ -204,7 +221,14 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
     HOLO_CUDA(cudaMemcpyAsync(st, stats, sizeof(st), cudaMemcpyDeviceToHost, s));
     HOLO_CUDA(cudaStreamSynchronize(s));
     variant = cands[i];
-    if (bound_from_stats(st) <= budget) break;
+    double curv = 0.0;
+    const double bound = bound_from_stats(st, &curv);
+    const int twin = no_correction_twin(cands[i]);
+    if (twin >= 0 && bound + curv <= budget) {
+      variant = twin;
+      break;
+    }
+    if (bound <= budget) break;
   }
   const Variant V = split_variant(variant);
   // the last bound evaluation left this variant's tile boxes in tiles_s / tiles_t

@@ -192,13 +192,15 @@ int holo_transform_batched(holo_handle h, const holo_problem *problems, int n_pr
                            int precision, holo_stream_t stream);
 
 /* ---- kernel variants and the autotuner -----------------------------------
- * Variants are (threads per CTA, targets per thread, sources per tile).  The
- * planner picks one per size bucket; holo_autotune times every variant on a
- * synthetic problem of the given size and records the fastest for its bucket.
- * The Python layer persists the table as JSON. */
+ * Variants are (threads per CTA, targets per thread, sources per tile, targets
+ * per thread whose sin/cos run on the FMA pipe, whether the per-pair curvature
+ * correction is kept).  The planner picks one per size bucket (dropping the
+ * curvature term only when its error bound allows); holo_autotune times every
+ * variant on a synthetic problem of the given size and records the fastest for
+ * its bucket.  The Python layer persists the table as JSON. */
 int holo_variant_count(int precision);
 int holo_variant_describe(int precision, int variant, int *threads, int *targets_per_thread,
-                          int *source_tile, int *fma_sincos_targets);
+                          int *source_tile, int *fma_sincos_targets, int *curvature_term);
 int holo_set_variant(holo_handle h, int precision, int bucket, int variant);
 int holo_get_variant(holo_handle h, int precision, int bucket, int *variant);
 int holo_size_bucket(size_t N, size_t M);

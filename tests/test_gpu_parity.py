@@ -190,3 +190,20 @@ def test_reference_wave_amplitude_only(holo, orc):
     expect_phase = np.angle(rn)
     assert np.max(np.abs(ya - expect_amp)) < 1e-10
     assert np.max(np.abs(np.angle(np.exp(1j * (yp - expect_phase))))) < 1e-10
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split32"])
+def test_every_kernel_variant(holo, orc, prec):
+    """Each kernel variant (tile shapes, FMA-pipe sin/cos share, curvature term on or off)
+    meets the precision target on a 32x32 -> 64x64 patch of the config-1 planes, both
+    signs.  The variants without the curvature term are exact enough here because the
+    planes are 0.35 m apart and the tiles are a fraction of a millimetre wide."""
+    rng = np.random.default_rng(11)
+    u, v = grid(32, 10e-6, 0.35), grid(64, 7.56e-6, 0.0)
+    amp, phase = rng.uniform(0, 1, len(u)), rng.uniform(0, 2 * np.pi, len(u))
+    refs = {s: orc.transform(amp, phase, u, v, s, LAM) for s in (-1, 1)}
+    for var in holo.variants(prec):
+        for s in (-1, 1):
+            y = holo.transform(amp, phase, u, v, s, LAM, precision=prec,
+                               variant=var["variant"])
+            assert rel_l2(y, refs[s]) < TOL[prec], (var, s)
