@@ -36,13 +36,16 @@ FLOP_PER_PAIR = 29   # the reference's FLOP_PER_POINT (cuda/macros.h:71-80)
 
 
 def pipe_ops_per_pair(variant: dict) -> tuple[float, float]:
-    """(MUFU ops, FP32-pipe ops) per pair of a split-kernel variant: 3 MUFU (rsqrt,
-    sin, cos) + 12 FP32 per pair (10 without the curvature correction), except that
-    `fma_sincos_targets` of every `targets_per_thread` take sin/cos from the
-    FMA-pipe polynomial (+16 FP32, -2 MUFU)."""
+    """(MUFU ops, FP32-pipe ops) per pair of a split-kernel variant, by pair model:
+    0 (curvature correction): 3 MUFU (rsqrt, sin, cos) + 12 FP32; 1 (without it):
+    3 + 10; 2 (1/q series, no rsqrt): 2 + 8.  `fma_sincos_targets` of every
+    `targets_per_thread` take sin/cos from the FMA-pipe polynomial instead
+    (+16 FP32, -2 MUFU)."""
     f = variant["fma_sincos_targets"] / variant["targets_per_thread"]
-    base = 12.0 if variant.get("curvature_term", 1) else 10.0
-    return 3.0 - 2.0 * f, base + 16.0 * f
+    mufu, fp32 = {0: (3.0, 12.0), 1: (3.0, 10.0), 2: (2.0, 8.0)}[variant.get("pair_model", 0)]
+    return mufu - 2.0 * f, fp32 + 16.0 * f
+
+
 WORKLOAD = "config2: 512^2 sources -> 1024^2 projector -> 512^2 projection (x->y->z)"
 
 

@@ -151,7 +151,8 @@ class Handle:
         return ms.value, n.value
 
     def probe_peak(self, kind: int) -> float:
-        """Measured lane-ops/s of the MUFU (kind 0) or FP32 FMA (kind 1) pipe."""
+        """Measured lane-instructions/s of the MUFU (kind 0), FP32 FMA (kind 1) or packed
+        FP32-pair FMA (kind 2, two FMAs each) pipe."""
         r = ctypes.c_double()
         N.check(self.lib.holo_probe_peak(self.h, kind, ctypes.byref(r)))
         return r.value
@@ -423,7 +424,7 @@ def variants(precision="split32") -> list[dict]:
                                         ctypes.byref(q), ctypes.byref(k)))
         out.append({"variant": i, "threads": t.value, "targets_per_thread": r.value,
                     "source_tile": c.value, "target_tile": t.value * r.value,
-                    "fma_sincos_targets": q.value, "curvature_term": k.value})
+                    "fma_sincos_targets": q.value, "pair_model": k.value})
     return out
 
 

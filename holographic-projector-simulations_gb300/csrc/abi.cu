@@ -216,23 +216,63 @@ static int sort_set(holo_plan_s *p, const double *pos, int n, int n_pad, double 
   return HOLO_OK;
 }
 
-// Tile boxes for source tiles of `cs` and target tiles of `tt` points, and a
-// bound (in metres) on the error of the split-precision path length r:
-//   c = |d_perp|^2 <= (hs + ht)^2 over the worst tile pair, r >= gap between
-//   the two point sets' boxes, rho = c / 2r the FP32 curvature term:
-//   FP32 rounding of rho (~4 ulp), of the in-tile offsets (c / r * 2^-24) and
-//   the truncated series term rho (c / r^2)^2 / 8.
+// Error model of the split path (declared in internal.cuh), in metres of path
+// length.  gap = distance between the two point sets' boxes (r >= gap),
+// c = |d_perp|^2 <= (h_s + h_t)^2 over the worst tile pair, rho = c / 2r:
+//   base = FP32 rounding of rho (~4 ulp) and of the in-tile offsets
+//          (c / r * 2^-24), and the truncated series term rho (c / r^2)^2 / 8;
+//   curv = c^2 / 8r^3 = rho (c / r^2) / 4;
+//   lin  = for 1/q ~ (1 + x) / Qt, x = Ps / Qt: the phase error rho x^2 / (1 - x)
+//          plus the relative amplitude error of 1/r ~ (1 + Ps / r0) / Qt,
+//          x^2 + c / 2q^2 + |Ps| h_t / (Qt r0), as the path length of the same
+//          phase at 400 nm.  |Ps| = |e.s'| <= sum_d |e_d| hd_s[d] with
+//          |e_d| <= min(1, span_d / gap) (span_d: the largest target-source
+//          coordinate difference along d), and Qt >= gap - h_t.
+void split_error_model(const TileStats &st, double *base, double *curv, double *lin) {
+  double gap2 = 0.0, ps = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    const double g = std::max(0.0, std::max(st.lo_s[d] - st.hi_t[d], st.lo_t[d] - st.hi_s[d]));
+    gap2 += g * g;
+  }
+  const double gap = sqrt(gap2);
+  if (!(gap > 0.0)) {
+    *base = *curv = *lin = INFINITY;
+    return;
+  }
+  for (int d = 0; d < 3; ++d) {
+    const double span = std::max(fabs(st.hi_t[d] - st.lo_s[d]), fabs(st.hi_s[d] - st.lo_t[d]));
+    ps += std::min(1.0, span / gap) * st.hd_s[d];
+  }
+  const double c = (st.h_s + st.h_t) * (st.h_s + st.h_t), rho = c / (2.0 * gap), y = c / gap2;
+  *base = rho * ldexp(1.0, -21) + c / gap * ldexp(1.0, -24) + rho * y * y / 8.0;
+  *curv = rho * y / 4.0;
+  const double qt = gap - st.h_t, x = qt > 0.0 ? ps / qt : INFINITY;
+  if (!(x < 0.5)) {
+    *lin = INFINITY;
+    return;
+  }
+  const double x2 = x * x / (1.0 - x);
+  *lin = rho * x2 + (x2 + y / 2.0 + ps * st.h_t / (qt * gap)) * (400e-9 / (2.0 * M_PI));
+}
+
+// Tile boxes for source tiles of `cs` and target tiles of `tt` points, and the
+// split-path error model of that tiling.
 static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, double *curv,
-                            cudaStream_t s) {
+                            double *lin, cudaStream_t s) {
   const int ns = (p->N + cs - 1) / cs, nt = (p->M + tt - 1) / tt;
   HOLO_TRY(launch_tile_bbox(p->pos_s, p->N, cs, p->tiles_s, s));
   HOLO_TRY(launch_tile_bbox(p->pos_t, p->M, tt, p->tiles_t, s));
+  if (ns == 0 || nt == 0) {
+    *bound = *curv = *lin = 0.0;
+    return HOLO_OK;
+  }
   std::vector<double> ts((size_t)6 * ns), tg((size_t)6 * nt);
-  if (ns) HOLO_CUDA(cudaMemcpyAsync(ts.data(), p->tiles_s, ts.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-  if (nt) HOLO_CUDA(cudaMemcpyAsync(tg.data(), p->tiles_t, tg.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  HOLO_CUDA(cudaMemcpyAsync(ts.data(), p->tiles_s, ts.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  HOLO_CUDA(cudaMemcpyAsync(tg.data(), p->tiles_t, tg.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
   HOLO_CUDA(cudaStreamSynchronize(s));
-  auto boxes = [](const std::vector<double> &t, int n, double *lo, double *hi, double *hmax) {
-    for (int d = 0; d < 3; ++d) { lo[d] = 1e300; hi[d] = -1e300; }
+  auto boxes = [](const std::vector<double> &t, int n, double *lo, double *hi, double *hmax,
+                  double *hd) {
+    for (int d = 0; d < 3; ++d) { lo[d] = 1e300; hi[d] = -1e300; hd[d] = 0.0; }
     *hmax = 0.0;
     for (int i = 0; i < n; ++i) {
       const double *c = &t[6 * (size_t)i];
@@ -240,41 +280,17 @@ static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, doubl
       for (int d = 0; d < 3; ++d) {
         lo[d] = std::min(lo[d], c[d] - c[3 + d]);
         hi[d] = std::max(hi[d], c[d] + c[3 + d]);
+        hd[d] = std::max(hd[d], c[3 + d]);
         h2 += c[3 + d] * c[3 + d];
       }
       *hmax = std::max(*hmax, sqrt(h2));
     }
   };
-  double slo[3], shi[3], tlo[3], thi[3], hs, ht;
-  boxes(ts, ns, slo, shi, &hs);
-  boxes(tg, nt, tlo, thi, &ht);
-  double gap2 = 0.0;
-  for (int d = 0; d < 3; ++d) {
-    const double g = std::max(0.0, std::max(slo[d] - thi[d], tlo[d] - shi[d]));
-    gap2 += g * g;
-  }
-  const double gap = sqrt(gap2);
-  if (!(gap > 0.0) || ns == 0 || nt == 0) {
-    *bound = ns && nt ? INFINITY : 0.0;
-    *curv = *bound;
-    return HOLO_OK;
-  }
-  const double c = (hs + ht) * (hs + ht), rho = c / (2.0 * gap), y = c / gap2;
-  *bound = rho * ldexp(1.0, -21) + c / gap * ldexp(1.0, -24) + rho * y * y / 8.0;
-  *curv = rho * y / 4.0;  // the curvature term c^2 / 8r^3 a variant may drop
+  TileStats st;
+  boxes(ts, ns, st.lo_s, st.hi_s, &st.h_s, st.hd_s);
+  boxes(tg, nt, st.lo_t, st.hi_t, &st.h_t, st.hd_t);
+  split_error_model(st, bound, curv, lin);
   return HOLO_OK;
-}
-
-// The variant with the same tiles that drops the curvature term (or -1).
-static int no_correction_twin(int v) {
-  const Variant A = split_variant(v);
-  if (!A.corr) return -1;
-  for (int i = 0; i < split_variant_count(); ++i) {
-    const Variant B = split_variant(i);
-    if (!B.corr && B.threads == A.threads && B.r == A.r && B.cs == A.cs && B.poly == A.poly)
-      return i;
-  }
-  return -1;
 }
 
 // Path-length error budget of the split path: 5e-6 rad at lambda = 400 nm.
@@ -317,16 +333,20 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
           cands.push_back(c);
     for (size_t i = 0; i < cands.size(); ++i) {
       const Variant C = split_variant(cands[i]);
-      double bound = 0.0, curv = 0.0;
-      HOLO_TRY(tile_error_bound(p.get(), C.cs, C.tt(), &bound, &curv, s));
+      double bound = 0.0, curv = 0.0, lin = 0.0;
+      HOLO_TRY(tile_error_bound(p.get(), C.cs, C.tt(), &bound, &curv, &lin, s));
+      const double model_bound[3] = {bound, bound + curv, bound + curv + lin};
       variant = cands[i];
-      p->err_bound = C.corr ? bound : bound + curv;
-      if (C.corr && forced_variant < 0) {
-        // the same tiles without the per-pair curvature term, when it is negligible
-        const int twin = no_correction_twin(cands[i]);
-        if (twin >= 0 && bound + curv <= kSplitBoundMetres) {
-          variant = twin;
-          p->err_bound = bound + curv;
+      p->err_bound = model_bound[C.model];
+      if (forced_variant < 0) {
+        // the same tiles with the cheapest pair model whose bound holds
+        for (int m = 2; m > C.model; --m) {
+          const int twin = split_twin(cands[i], m);
+          if (twin >= 0 && model_bound[m] <= kSplitBoundMetres) {
+            variant = twin;
+            p->err_bound = model_bound[m];
+            break;
+          }
         }
       }
       if (p->err_bound <= kSplitBoundMetres) break;
@@ -1003,7 +1023,7 @@ int holo_variant_count(int precision) {
 }
 
 int holo_variant_describe(int precision, int variant, int *threads, int *targets_per_thread,
-                          int *source_tile, int *fma_sincos_targets, int *curvature_term) {
+                          int *source_tile, int *fma_sincos_targets, int *pair_model) {
   const int n = holo_variant_count(precision);
   if (n < 0) return n;
   if (variant < 0 || variant >= n) return fail(HOLO_ERR_INVALID, "variant %d out of range", variant);
@@ -1012,7 +1032,7 @@ int holo_variant_describe(int precision, int variant, int *threads, int *targets
   if (targets_per_thread) *targets_per_thread = V.r;
   if (source_tile) *source_tile = V.cs;
   if (fma_sincos_targets) *fma_sincos_targets = V.poly;
-  if (curvature_term) *curvature_term = V.corr;
+  if (pair_model) *pair_model = V.model;
   return HOLO_OK;
 }
 

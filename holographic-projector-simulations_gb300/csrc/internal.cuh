@@ -59,13 +59,38 @@ struct Variant {
   int r;        // targets per thread (register blocking)
   int cs;       // sources per tile (one bulk copy per tile)
   int poly = 0; // targets per thread whose sin/cos run on the FMA pipe
-  int corr = 1; // 1: per-pair curvature correction c^2 / 8r^3; 0: dropped (the
-                // planner picks such a variant only when its error bound allows)
+  int model = 0; // per-pair model of the curvature term rho and of 1/r:
+                 //   0: c / 2r (1 + c / 4r^2) with r from rsqrt (12 FP32 + 3 MUFU)
+                 //   1: c / 2r, rsqrt                             (10 FP32 + 3 MUFU)
+                 //   2: c / 2q with 1/q to first order in Ps / Qt  (8 FP32 + 2 MUFU)
+                 // the planner takes model 1 or 2 only when its error bound allows
+  int packed = 0; // 1: pair loop on packed FP32 pairs (two sources per instruction)
   int tt() const { return threads * r; }
 };
 
 int split_variant_count();
 Variant split_variant(int i);
+// The variant with the same tiles and sin/cos split as `v` and pair model
+// `model` (its packed pair loop where there is one), or -1.
+int split_twin(int v, int model);
+
+// Largest tile boxes of a source and a target tiling: per set the bounding box
+// of all tiles (lo, hi), the largest tile half-diagonal h and the largest
+// half-extent along each axis hd.
+struct TileStats {
+  double lo_s[3], hi_s[3], h_s, hd_s[3];
+  double lo_t[3], hi_t[3], h_t, hd_t[3];
+};
+
+// Error model of the split path (metres of path length) for one tiling:
+//   base: FP32 rounding of the curvature term and of the in-tile offsets, and the
+//         series truncation of pair model 0;
+//   curv: the curvature term c^2 / 8r^3 that pair models 1 and 2 drop;
+//   lin:  the extra error of pair model 2 (1/q to first order in Ps / Qt, and
+//         1/q for the amplitude 1/r), its amplitude part as the phase (radians at
+//         400 nm) of the same size.
+// Infinite when the two point sets' boxes touch.
+void split_error_model(const TileStats &st, double *base, double *curv, double *lin);
 int fp64_variant_count();
 Variant fp64_variant(int i);
 

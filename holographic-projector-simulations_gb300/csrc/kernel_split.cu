@@ -19,10 +19,12 @@
 // frame itself (one thread per tile pair) is FP64.  Per pair only the small
 // curvature term s k rho (|rho| / r0 ~ 1e-6) and the amplitude 1/r are formed
 // in FP32; their sensitivity to FP32 rounding of d is suppressed by |d| / r0.
-// Per pair: 12 FP32 ops + 3 MUFU ops (rsqrt, sin, cos); POLY of the R targets
-// per thread take sin/cos from an FMA-pipe polynomial instead (17 FP32 ops,
-// 1 MUFU).  Sums run in FP32 over one source tile (CS terms), are rotated by
-// e^{iB} and carried in FP64.
+// Per pair: 12 FP32 ops + 3 MUFU ops (rsqrt, sin, cos); 10 + 3 without the
+// curvature correction, 8 + 2 with 1/r replaced by a first-order series of 1/q
+// (pair models 0, 1, 2: the planner takes 1 or 2 only where the error bound of
+// the tiling allows).  POLY of the R targets per thread take sin/cos from an
+// FMA-pipe polynomial instead (+16 FP32 ops, -2 MUFU).  Sums run in FP32 over
+// one source tile (CS terms), are rotated by e^{iB} and carried in FP64.
 #include "internal.cuh"
 #include "ptx.cuh"
 
@@ -163,6 +165,34 @@ __device__ __forceinline__ void poly_sincos(float th, float *sn, float *cs) {
   *cs = c;
 }
 
+// Both halves of a packed pair set to one compile-time constant.
+__device__ __forceinline__ uint64_t splat2(float k) {
+  const uint64_t b = __float_as_uint(k);
+  return (b << 32) | b;
+}
+
+// poly_sincos on a packed pair of angles (fma.rn.f32x2 and friends): the same
+// polynomial and operation order as poly_sincos, two angles per instruction.
+__device__ __forceinline__ void poly_sincos2(uint64_t th, uint64_t &sn, uint64_t &cs) {
+  const uint64_t t = ptx::mul2(th, splat2(0.159154943f));
+  const uint64_t n = ptx::sub2(ptx::add2(t, splat2(12582912.0f)), splat2(12582912.0f));
+  const uint64_t f = ptx::sub2(t, n);
+  const uint64_t f2 = ptx::mul2(f, f);
+  uint64_t s = ptx::fma2(splat2(-1.227126217e+01f), f2, splat2(4.120539474e+01f));
+  s = ptx::fma2(s, f2, splat2(-7.658010101e+01f));
+  s = ptx::fma2(s, f2, splat2(8.159618378e+01f));
+  s = ptx::fma2(s, f2, splat2(-4.134142303e+01f));
+  s = ptx::fma2(s, f2, splat2(6.283182621e+00f));
+  uint64_t c = ptx::fma2(splat2(6.529610157e+00f), f2, splat2(-2.596831322e+01f));
+  c = ptx::fma2(c, f2, splat2(6.016783142e+01f));
+  c = ptx::fma2(c, f2, splat2(-8.545016479e+01f));
+  c = ptx::fma2(c, f2, splat2(6.493911743e+01f));
+  c = ptx::fma2(c, f2, splat2(-1.973920441e+01f));
+  c = ptx::fma2(c, f2, splat2(1.0f));
+  sn = ptx::mul2(s, f);
+  cs = c;
+}
+
 // One staging buffer of source records (float-float offsets + (phase, amp)):
 // the bulk copy of tile j+1 is issued once the frame phase of tile j has
 // consumed it, so it overlaps tile j's pair loop.
@@ -212,15 +242,31 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
   const double sk = P.sk;
   const float kap2 = (float)(0.5 * sk);    // s k / 2
   const int n_strata = MC ? (P.N + P.sub - 1) / P.sub : 0;
-  // POLY = (targets per thread on the FMA-pipe sin/cos) | 16 * (no curvature
-  // correction).  Without the correction the curvature quantities are stored
-  // scaled: c_s = kap2^2 c, q_s = |kap2| q, so r2_s = q_s^2 + c_s = kap2^2 r^2 and
-  // the phase is one FMA, theta' = c_s rsqrt(r2_s) + sign A, where theta =
-  // sign theta' (the sign flips the imaginary part at the end) and the
-  // amplitude a |kap2| absorbs the 1 / |kap2| of rsqrt(r2_s).
+  // POLY = (targets per thread on the FMA-pipe sin/cos) | 16 (pair model 1) or
+  // | 32 (pair model 2); neither bit: model 0, with the curvature correction.
+  // Model 1 stores the curvature quantities scaled: c_s = kap2^2 c, q_s =
+  // |kap2| q, so r2_s = q_s^2 + c_s = kap2^2 r^2 and the phase is one FMA,
+  // theta' = c_s rsqrt(r2_s) + sign A, where theta = sign theta' (the sign
+  // flips the imaginary part at the end) and the amplitude a |kap2| absorbs
+  // the 1 / |kap2| of rsqrt(r2_s).
+  // Model 2 replaces 1/r by 1/q = 1 / (Qt - Ps) ~ (1 + Ps / Qt) / Qt: with
+  // iq = |kap2| / Qt + Ps |kap2| / Qt^2 (one FMA of per-target constants),
+  // theta' = c iq + sign A.  c / 2q is the curvature term rho = c / (q + r) to
+  // the same order as c / 2r (error c^2 / 8q^3 against c^2 / 8r^3).  The
+  // amplitude 1/r ~ 1/q ~ (1 + Ps / r0) / Qt (relative error c / 2q^2 +
+  // |Ps| |Qt - r0| / (Qt r0) + (Ps / Qt)^2) is split into a per-source factor,
+  // folded into the record, and 1 / Qt, applied to the tile sum per target.
+  // | 64 (model 2 only): the pair loop runs on packed FP32 pairs (f32x2), one
+  // instruction for the same target and two consecutive sources, the records
+  // stored pairwise: (qx, qx', qy, qy'), (qz, qz', qw, qw'), (a, a', S2, S2').
+  // Model 2 per pair: 7 FP32 ops (c: 3, iq, theta, two accumulations) + the
+  // sin/cos.
   constexpr int NPOLY = POLY & 15;
-  constexpr bool CORR = (POLY & 16) == 0;
-  const float ak = fabsf(kap2), ak2 = kap2 * kap2;
+  constexpr bool LIN = (POLY & 32) != 0;
+  constexpr bool CORR = (POLY & 48) == 0;
+  constexpr bool PK = (POLY & 64) != 0;
+  static_assert(!PK || LIN, "packed pair loop: pair model 2 only");
+  const float ak = fabsf(kap2), ak2 = kap2 * kap2, iak = 1.f / fabsf(kap2);
   const float sgn = kap2 < 0.f ? -1.f : 1.f;
 
   auto issue = [&](int j) {
@@ -276,6 +322,7 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
     const float f1x = fr->e1[0], f1y = fr->e1[1], f1z = fr->e1[2];
     const float f2x = fr->e2[0], f2y = fr->e2[1], f2z = fr->e2[2];
     const float fex = fr->ef[0], fey = fr->ef[1], fez = fr->ef[2];
+    const float ir0 = fr->r0f > 0.f ? 1.f / fr->r0f : 0.f;
     float ah[3], al[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -329,16 +376,32 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
         if (CORR || CONST) {
           q = make_float4(-2.f * Sx, -2.f * Sy, Ps, A);
           a = make_float2(am, fmaf(Sx, Sx, Sy * Sy));
+        } else if (LIN) {
+          q = make_float4(-2.f * Sx, -2.f * Sy, Ps, sgn * A);
+          a = make_float2(am * fmaf(Ps, ir0, 1.f), fmaf(Sx, Sx, Sy * Sy));
         } else {
           q = make_float4(-2.f * ak2 * Sx, -2.f * ak2 * Sy, ak * Ps, sgn * A);
           a = make_float2(am * ak, ak2 * fmaf(Sx, Sx, Sy * Sy));
         }
       } else {
-        q = make_float4(0.f, 0.f, -1e18f, 0.f);  // r ~ 1e18: contributes 0
+        // padding: zero amplitude at the frame origin (finite terms times 0)
+        q = make_float4(0.f, 0.f, 0.f, 0.f);
         a = make_float2(0.f, 0.f);
       }
-      rec[i] = q;
-      ramp[i] = a;
+      if (PK) {
+        float *pa = reinterpret_cast<float *>(rec), *pb = pa + 2 * CS;
+        float *pc = reinterpret_cast<float *>(ramp);
+        const int o = 4 * (i >> 1) + (i & 1);
+        pa[o] = q.x;
+        pa[o + 2] = q.y;
+        pb[o] = q.z;
+        pb[o + 2] = q.w;
+        pc[o] = a.x;
+        pc[o + 2] = a.y;
+      } else {
+        rec[i] = q;
+        ramp[i] = a;
+      }
     }
 
     // ---- per-thread target frame (FP32 pipe, float-float for B) ----
@@ -365,7 +428,12 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       // curvature correction s k c^2 / (8 r^3) = h * c * (s k / 8) / r^2 with
       // 1/r^2 taken as 1/Qt^2 (relative error ~2 |Ps| / r0 of a ~1e-6 rad term)
       kq[r] = __fdividef(0.25f * kap2, Qt[r] * Qt[r]);
-      if (!CORR && !CONST) {
+      if (LIN && !CONST) {
+        // Qt[r] <- |kap2| / Qt and kq[r] <- |kap2| / Qt^2 (correctly rounded)
+        const float iq = ak / Qt[r];
+        kq[r] = iq / Qt[r];
+        Qt[r] = iq;
+      } else if (!CORR && !CONST) {
         Qt[r] *= ak;
         T2[r] *= ak2;
       }
@@ -382,37 +450,102 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       re[r] = 0.f;
       im[r] = 0.f;
     }
-#pragma unroll 2
-    for (int s = 0; s < count; ++s) {
-      const float4 q = rec[s];
-      const float2 as = ramp[s];
-      if (CONST) {
+    if (PK) {
+      // two consecutive sources per instruction; an odd count reads one padding
+      // record (zero amplitude), so (count + 1) / 2 pairs cover the tile
+      const float4 *pa = reinterpret_cast<const float4 *>(rec), *pb = pa + CS / 2;
+      const float4 *pc = reinterpret_cast<const float4 *>(ramp);
+      const int npair = (count + 1) >> 1;
+      uint64_t tx2[R], ty2[R], t22[R], iq2[R], kq2[R], re2[R], im2[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) re[r] += as.x;
-      } else {
+      for (int r = 0; r < R; ++r) {
+        tx2[r] = ptx::pack2(Tx[r], Tx[r]);
+        ty2[r] = ptx::pack2(Ty[r], Ty[r]);
+        t22[r] = ptx::pack2(T2[r], T2[r]);
+        iq2[r] = ptx::pack2(Qt[r], Qt[r]);
+        kq2[r] = ptx::pack2(kq[r], kq[r]);
+        re2[r] = 0ull;
+        im2[r] = 0ull;
+      }
+#pragma unroll 2
+      for (int p = 0; p < npair; ++p) {
+        const float4 c4 = pc[p];
+        if (CONST) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) re[r] += c4.x + c4.y;
+        } else {
+          const float4 a4 = pa[p], b4 = pb[p];
+          const uint64_t qx = ptx::pack2(a4.x, a4.y), qy = ptx::pack2(a4.z, a4.w);
+          const uint64_t qz = ptx::pack2(b4.x, b4.y), qw = ptx::pack2(b4.z, b4.w);
+          const uint64_t am = ptx::pack2(c4.x, c4.y), s2 = ptx::pack2(c4.z, c4.w);
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const uint64_t c = ptx::fma2(tx2[r], qx, ptx::fma2(ty2[r], qy, ptx::add2(t22[r], s2)));
+            const uint64_t iq = ptx::fma2(qz, kq2[r], iq2[r]);  // |kap2| / q, first order
+            const uint64_t th = ptx::fma2(c, iq, qw);           // sign * theta
+            uint64_t sn, cs;
+            if (r < NPOLY) {
+              poly_sincos2(th, sn, cs);  // FMA pipe
+            } else {
+              float t0, t1;
+              ptx::unpack2(th, t0, t1);
+              sn = ptx::pack2(ptx::sin_approx(t0), ptx::sin_approx(t1));  // XU pipe
+              cs = ptx::pack2(ptx::cos_approx(t0), ptx::cos_approx(t1));
+            }
+            re2[r] = ptx::fma2(am, cs, re2[r]);
+            im2[r] = ptx::fma2(am, sn, im2[r]);
+          }
+        }
+      }
+      if (!CONST) {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          const float c = fmaf(Tx[r], q.x, fmaf(Ty[r], q.y, T2[r] + as.y));
-          const float qq = Qt[r] - q.z;
-          const float r2 = fmaf(qq, qq, c);
-          const float ir = ptx::rsqrt_approx(r2);
-          float th;
-          if (CORR) {
-            const float h = c * ir;
-            th = fmaf(h, fmaf(c, kq[r], kap2), q.w);
-          } else {
-            th = fmaf(c, ir, q.w);  // scaled: sign * theta
+          float a, b;
+          ptx::unpack2(re2[r], a, b);
+          re[r] = a + b;
+          ptx::unpack2(im2[r], a, b);
+          im[r] = a + b;
+        }
+      }
+    } else {
+#pragma unroll 2
+      for (int s = 0; s < count; ++s) {
+        const float4 q = rec[s];
+        const float2 as = ramp[s];
+        if (CONST) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) re[r] += as.x;
+        } else {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const float c = fmaf(Tx[r], q.x, fmaf(Ty[r], q.y, T2[r] + as.y));
+            float th, w;
+            if (LIN) {
+              const float iq = fmaf(q.z, kq[r], Qt[r]);  // |kap2| / q to first order
+              th = fmaf(c, iq, q.w);                     // sign * theta
+              w = as.x;                                  // 1 / Qt after the sum
+            } else {
+              const float qq = Qt[r] - q.z;
+              const float r2 = fmaf(qq, qq, c);
+              const float ir = ptx::rsqrt_approx(r2);
+              if (CORR) {
+                const float h = c * ir;
+                th = fmaf(h, fmaf(c, kq[r], kap2), q.w);
+              } else {
+                th = fmaf(c, ir, q.w);  // scaled: sign * theta
+              }
+              w = as.x * ir;
+            }
+            float sn, cs;
+            if (r < NPOLY) {
+              poly_sincos(th, &sn, &cs);  // FMA pipe
+            } else {
+              sn = ptx::sin_approx(th);   // XU (MUFU) pipe
+              cs = ptx::cos_approx(th);
+            }
+            re[r] = fmaf(w, cs, re[r]);
+            im[r] = fmaf(w, sn, im[r]);
           }
-          const float w = as.x * ir;
-          float sn, cs;
-          if (r < NPOLY) {
-            poly_sincos(th, &sn, &cs);  // FMA pipe
-          } else {
-            sn = ptx::sin_approx(th);   // XU (MUFU) pipe
-            cs = ptx::cos_approx(th);
-          }
-          re[r] = fmaf(w, cs, re[r]);
-          im[r] = fmaf(w, sn, im[r]);
         }
       }
     }
@@ -425,9 +558,10 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       } else {
         float sb, cb;
         __sincosf(bph[r * THREADS + tid], &sb, &cb);
-        const float imr = CORR ? im[r] : sgn * im[r];
-        a.x += (double)fmaf(re[r], cb, -imr * sb);
-        a.y += (double)fmaf(re[r], sb, imr * cb);
+        const float sc = LIN ? Qt[r] * iak : 1.f;  // model 2: 1 / Qt
+        const float rer = re[r] * sc, imr = (CORR ? im[r] : sgn * im[r]) * sc;
+        a.x += (double)fmaf(rer, cb, -imr * sb);
+        a.y += (double)fmaf(rer, sb, imr * cb);
       }
       acc[r * THREADS + tid] = a;
     }
@@ -520,11 +654,23 @@ constexpr Variant kVariants[] = {
     {256, 8, 1024, 4},  // 10: as 0, 4 of 8
     {256, 4, 512, 1},   // 11: 3 CTAs/SM
     {128, 4, 512, 1},   // 12: 5 CTAs/SM
-    // without the curvature correction (10 FP32 ops + 3 MUFU per pair)
-    {256, 4, 1024, 1, 0},  // 13: as 9
-    {256, 8, 1024, 2, 0},  // 14: as 7
-    {256, 8, 1024, 3, 0},  // 15: as 8
-    {256, 4, 512, 1, 0},   // 16: as 11
+    // pair model 1: no curvature correction (10 FP32 ops + 3 MUFU per pair)
+    {256, 4, 1024, 1, 1},  // 13: as 9
+    {256, 8, 1024, 2, 1},  // 14: as 7
+    {256, 8, 1024, 3, 1},  // 15: as 8
+    {256, 4, 512, 1, 1},   // 16: as 11
+    // pair model 2: 1/q to first order, no rsqrt (8 FP32 ops + 2 MUFU per pair)
+    {256, 4, 1024, 1, 2},  // 17: as 9
+    {256, 4, 1024, 0, 2},  // 18: as 2
+    {256, 8, 1024, 1, 2},  // 19: as 6
+    {256, 8, 1024, 2, 2},  // 20: as 7
+    {256, 4, 512, 1, 2},   // 21: as 11
+    // pair model 2 on packed FP32 pairs (f32x2: two sources per instruction)
+    {256, 4, 1024, 0, 2, 1},  // 22: as 18
+    {256, 4, 1024, 1, 2, 1},  // 23: as 17
+    {256, 4, 1024, 2, 2, 1},  // 24: 2 of 4 targets on the FMA-pipe sin/cos
+    {256, 2, 1024, 1, 2, 1},  // 25: TT 512, 1 of 2
+    {128, 4, 1024, 1, 2, 1},  // 26: TT 512, 1 of 4
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -577,6 +723,19 @@ int occupancy_variant(bool mc, int *out) {
 int split_variant_count() { return kNumVariants; }
 Variant split_variant(int i) { return kVariants[i]; }
 
+int split_twin(int v, int model) {
+  if (v < 0 || v >= kNumVariants) return -1;
+  const Variant &A = kVariants[v];
+  int best = -1;
+  for (int i = 0; i < kNumVariants; ++i) {
+    const Variant &B = kVariants[i];
+    if (B.model == model && B.threads == A.threads && B.r == A.r && B.cs == A.cs &&
+        B.poly == A.poly && (best < 0 || B.packed > kVariants[best].packed))
+      best = i;  // the packed pair loop where there is one
+  }
+  return best;
+}
+
 #define HOLO_SPLIT_DISPATCH(V, CALL)                      \
   switch (V) {                                            \
     case 0: return CALL(256, 8, 1024, 0);                 \
@@ -596,6 +755,16 @@ Variant split_variant(int i) { return kVariants[i]; }
     case 14: return CALL(256, 8, 1024, 2 | 16);           \
     case 15: return CALL(256, 8, 1024, 3 | 16);           \
     case 16: return CALL(256, 4, 512, 1 | 16);            \
+    case 17: return CALL(256, 4, 1024, 1 | 32);           \
+    case 18: return CALL(256, 4, 1024, 0 | 32);           \
+    case 19: return CALL(256, 8, 1024, 1 | 32);           \
+    case 20: return CALL(256, 8, 1024, 2 | 32);           \
+    case 21: return CALL(256, 4, 512, 1 | 32);            \
+    case 22: return CALL(256, 4, 1024, 0 | 96);           \
+    case 23: return CALL(256, 4, 1024, 1 | 96);           \
+    case 24: return CALL(256, 4, 1024, 2 | 96);           \
+    case 25: return CALL(256, 2, 1024, 1 | 96);           \
+    case 26: return CALL(128, 4, 1024, 1 | 96);           \
     default: return fail(HOLO_ERR_INVALID, "unknown split variant %d", V); \
   }
 

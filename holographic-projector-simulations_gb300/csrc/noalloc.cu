@@ -57,8 +57,8 @@ int noalloc_scratch(int device, unsigned char **out) {
   return HOLO_OK;
 }
 
-// Reduce the tile boxes of both point sets to 14 numbers: source box lo/hi,
-// largest source tile half-diagonal, target box lo/hi, largest target one.
+// Reduce the tile boxes of both point sets to 20 numbers, 10 per set: box
+// lo/hi, largest tile half-diagonal, largest half-extent along each axis.
 __global__ void __launch_bounds__(256) k_tile_stats(const double *__restrict__ ts, int ns,
                                                     const double *__restrict__ tt, int nt,
                                                     double *__restrict__ out) {
@@ -66,15 +66,15 @@ __global__ void __launch_bounds__(256) k_tile_stats(const double *__restrict__ t
   const double *tiles[2] = {ts, tt};
   const int counts[2] = {ns, nt};
   for (int set = 0; set < 2; ++set) {
-    for (int q = 0; q < 7; ++q) {  // 3 lo (min), 3 hi (max), half-diagonal (max)
+    for (int q = 0; q < 10; ++q) {  // 3 lo (min), 3 hi, half-diagonal, 3 half-extents (max)
       const bool is_min = q < 3;
-      double v = is_min ? 1e300 : -1e300;
-      if (q == 6) v = 0.0;
+      double v = is_min ? 1e300 : (q < 6 ? -1e300 : 0.0);
       for (int i = threadIdx.x; i < counts[set]; i += blockDim.x) {
         const double *c = tiles[set] + 6 * (size_t)i;
         if (q < 3) v = fmin(v, c[q] - c[3 + q]);
         else if (q < 6) v = fmax(v, c[q - 3] + c[q]);
-        else v = fmax(v, sqrt(c[3] * c[3] + c[4] * c[4] + c[5] * c[5]));
+        else if (q == 6) v = fmax(v, sqrt(c[3] * c[3] + c[4] * c[4] + c[5] * c[5]));
+        else v = fmax(v, c[q - 4]);
       }
       red[threadIdx.x] = v;
       __syncthreads();
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(256) k_tile_stats(const double *__restrict__ t
                                     : fmax(red[threadIdx.x], red[threadIdx.x + w]);
         __syncthreads();
       }
-      if (threadIdx.x == 0) out[7 * set + q] = red[0];
+      if (threadIdx.x == 0) out[10 * set + q] = red[0];
       __syncthreads();
     }
   }
@@ -103,35 +103,20 @@ struct Carve {
   }
 };
 
-// Path-length error bound (metres) from the 14 tile statistics, and the
-// curvature term c^2 / 8r^3 a variant may drop: the same model as the planner
-// of the allocating entry points.
-double bound_from_stats(const double *st, double *curv) {
-  double gap2 = 0.0;
+// The error model of the allocating planner, from the 20 tile statistics.
+void model_from_stats(const double *st, double *base, double *curv, double *lin) {
+  TileStats t;
   for (int d = 0; d < 3; ++d) {
-    const double g = std::max(0.0, std::max(st[d] - st[7 + 3 + d], st[7 + d] - st[3 + d]));
-    gap2 += g * g;
+    t.lo_s[d] = st[d];
+    t.hi_s[d] = st[3 + d];
+    t.hd_s[d] = st[7 + d];
+    t.lo_t[d] = st[10 + d];
+    t.hi_t[d] = st[13 + d];
+    t.hd_t[d] = st[17 + d];
   }
-  const double gap = sqrt(gap2);
-  if (!(gap > 0.0)) {
-    *curv = INFINITY;
-    return INFINITY;
-  }
-  const double c = (st[6] + st[13]) * (st[6] + st[13]), rho = c / (2.0 * gap), y = c / gap2;
-  *curv = rho * y / 4.0;
-  return rho * ldexp(1.0, -21) + c / gap * ldexp(1.0, -24) + rho * y * y / 8.0;
-}
-
-// The variant with the same tiles that drops the curvature term (or -1).
-int no_correction_twin(int v) {
-  const Variant A = split_variant(v);
-  for (int i = 0; i < split_variant_count(); ++i) {
-    const Variant B = split_variant(i);
-    if (A.corr && !B.corr && B.threads == A.threads && B.r == A.r && B.cs == A.cs &&
-        B.poly == A.poly)
-      return i;
-  }
-  return -1;
+  t.h_s = st[6];
+  t.h_t = st[16];
+  split_error_model(t, base, curv, lin);
 }
 
 bool is_device_pointer(const void *p) {
@@ -170,7 +155,7 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
   const int n_pad = (int)((N + 1023) / 1024) * 1024;
   Carve cv{base};
   int *err = cv.take<int>(16);
-  double *stats = cv.take<double>(16);
+  double *stats = cv.take<double>(20);
   double *pos_s = cv.take<double>(3 * (size_t)n_pad);
   int32_t *order_s = cv.take<int32_t>(N);
   double *pos_t = cv.take<double>(3 * M);
@@ -217,18 +202,24 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
     HOLO_TRY(launch_tile_bbox(pos_t, (int)M, C.tt(), tiles_t, s));
     k_tile_stats<<<1, 256, 0, s>>>(tiles_s, ns, tiles_t, nt, stats);
     HOLO_CUDA(cudaGetLastError());
-    double st[14];
+    double st[20];
     HOLO_CUDA(cudaMemcpyAsync(st, stats, sizeof(st), cudaMemcpyDeviceToHost, s));
     HOLO_CUDA(cudaStreamSynchronize(s));
+    double base = 0.0, curv = 0.0, lin = 0.0;
+    model_from_stats(st, &base, &curv, &lin);
+    const double model_bound[3] = {base, base + curv, base + curv + lin};
     variant = cands[i];
-    double curv = 0.0;
-    const double bound = bound_from_stats(st, &curv);
-    const int twin = no_correction_twin(cands[i]);
-    if (twin >= 0 && bound + curv <= budget) {
-      variant = twin;
-      break;
+    bool ok = model_bound[0] <= budget;
+    // the same tiles with the cheapest pair model whose bound holds
+    for (int m = 2; m > 0; --m) {
+      const int twin = split_twin(cands[i], m);
+      if (twin >= 0 && model_bound[m] <= budget) {
+        variant = twin;
+        ok = true;
+        break;
+      }
     }
-    if (bound <= budget) break;
+    if (ok) break;
   }
   const Variant V = split_variant(variant);
   // the last bound evaluation left this variant's tile boxes in tiles_s / tiles_t

@@ -63,6 +63,27 @@ __global__ void __launch_bounds__(256) k_probe_ffma(float *out, int iters, float
   if (s == 12345.f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// packed pairs: one fma.rn.f32x2 = two FP32 FMAs
+__global__ void __launch_bounds__(256) k_probe_ffma2(float *out, int iters, float seed) {
+  uint64_t x[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    x[j] = ptx::pack2(seed + 0.001f * (threadIdx.x + j), seed - 0.001f * (threadIdx.x + j));
+  const uint64_t a = ptx::pack2(0.999f, 0.998f), b = ptx::pack2(0.0001f, 0.0002f);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = ptx::fma2(x[j], a, b);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float lo, hi;
+    ptx::unpack2(x[j], lo, hi);
+    s += lo + hi;
+  }
+  if (s == 12345.f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
 }  // namespace holo
 
@@ -107,10 +128,12 @@ int holo_profile_end(holo_handle h, double *total_ms, int *launches) {
   return HOLO_OK;
 }
 
-// kind 0: MUFU sin.approx.f32 ops/s, kind 1: FP32 FMA ops/s (one op = one lane-instruction)
+// kind 0: MUFU sin.approx.f32 ops/s, kind 1: FP32 FMA ops/s (one op = one
+// lane-instruction), kind 2: packed fma.rn.f32x2 lane-instructions/s (each is
+// two FMAs)
 int holo_probe_peak(holo_handle h, int kind, double *ops_per_s) {
   if (!h || !ops_per_s) return fail(HOLO_ERR_INVALID, "null argument");
-  if (kind != 0 && kind != 1) return fail(HOLO_ERR_INVALID, "unknown probe %d", kind);
+  if (kind < 0 || kind > 2) return fail(HOLO_ERR_INVALID, "unknown probe %d", kind);
   std::lock_guard<std::mutex> lk(h->mu);
   int prev = -1;
   cudaGetDevice(&prev);
@@ -126,7 +149,8 @@ int holo_probe_peak(holo_handle h, int kind, double *ops_per_s) {
   for (int rep = 0; rep < 4; ++rep) {
     cudaEventRecord(e0);
     if (kind == 0) k_probe_mufu<<<blocks, threads>>>(out, iters, 0.1f + rep);
-    else k_probe_ffma<<<blocks, threads>>>(out, iters, 0.1f + rep);
+    else if (kind == 1) k_probe_ffma<<<blocks, threads>>>(out, iters, 0.1f + rep);
+    else k_probe_ffma2<<<blocks, threads>>>(out, iters, 0.1f + rep);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0.f;

@@ -193,14 +193,18 @@ int holo_transform_batched(holo_handle h, const holo_problem *problems, int n_pr
 
 /* ---- kernel variants and the autotuner -----------------------------------
  * Variants are (threads per CTA, targets per thread, sources per tile, targets
- * per thread whose sin/cos run on the FMA pipe, whether the per-pair curvature
- * correction is kept).  The planner picks one per size bucket (dropping the
- * curvature term only when its error bound allows); holo_autotune times every
- * variant on a synthetic problem of the given size and records the fastest for
- * its bucket.  The Python layer persists the table as JSON. */
+ * per thread whose sin/cos run on the FMA pipe, pair model).  The pair model of
+ * a HOLO_SPLIT32 variant says how the curvature term and 1/r are formed per
+ * pair: 0 = with the curvature correction c^2/8r^3, 1 = without it, 2 = without
+ * it and with 1/r replaced by a first-order series of 1/q (no rsqrt); it is 0
+ * for every HOLO_FP64 variant.  The planner picks one tile shape per size
+ * bucket, then the cheapest pair model whose error bound holds for the point
+ * sets; holo_autotune times every variant on a synthetic problem of the given
+ * size and records the fastest for its bucket.  The Python layer persists the
+ * table as JSON. */
 int holo_variant_count(int precision);
 int holo_variant_describe(int precision, int variant, int *threads, int *targets_per_thread,
-                          int *source_tile, int *fma_sincos_targets, int *curvature_term);
+                          int *source_tile, int *fma_sincos_targets, int *pair_model);
 int holo_set_variant(holo_handle h, int precision, int bucket, int variant);
 int holo_get_variant(holo_handle h, int precision, int bucket, int *variant);
 int holo_size_bucket(size_t N, size_t M);
@@ -214,7 +218,8 @@ int holo_autotune(holo_handle h, int precision, size_t N, size_t M, int repeats,
  * holo_profile_begin/end: CUDA-event time of every pair-evaluation kernel
  * launched on the handle in between (end synchronises those events).
  * holo_probe_peak: measured issue rate of this GPU's pipes, kind 0 = MUFU
- * (sin.approx.f32, the XU pipe), kind 1 = FP32 FMA, in lane-ops per second. */
+ * (sin.approx.f32, the XU pipe), kind 1 = FP32 FMA, kind 2 = packed FP32 pair
+ * FMA (fma.rn.f32x2, two FMAs each), in lane-instructions per second. */
 int holo_kernel_launches(long long *out);
 int holo_profile_begin(holo_handle h);
 int holo_profile_end(holo_handle h, double *total_ms, int *launches);
