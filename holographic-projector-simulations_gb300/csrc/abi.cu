@@ -293,8 +293,6 @@ static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, doubl
   return HOLO_OK;
 }
 
-// Path-length error budget of the split path: 5e-6 rad at lambda = 400 nm.
-constexpr double kSplitBoundMetres = 5e-6 * 400e-9 / (2.0 * M_PI);
 
 int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, size_t M,
                      int precision, int forced_variant, cudaStream_t s, holo_plan_s **out) {
@@ -336,6 +334,7 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
       double bound = 0.0, curv = 0.0, lin = 0.0;
       HOLO_TRY(tile_error_bound(p.get(), C.cs, C.tt(), &bound, &curv, &lin, s));
       const double model_bound[3] = {bound, bound + curv, bound + curv + lin};
+      for (int m = 0; m < 3; ++m) p->model_bounds[m] = model_bound[m];
       variant = cands[i];
       p->err_bound = model_bound[C.model];
       if (forced_variant < 0) {

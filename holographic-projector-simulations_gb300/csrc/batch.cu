@@ -1,12 +1,14 @@
-// batch.cu -- many independent problems of uneven size in one persistent launch.
+// batch.cu -- many independent problems of uneven size in persistent launches.
 //
 // The reference only loops over planes sequentially (cuda/main.cu:125-199),
-// one transform_full per plane.  Here every problem is planned once, its
-// (target tile, source range) work items go into one device work queue sorted
-// longest-first, and a persistent split-precision kernel drains the queue with
-// an atomic counter (no CTA waits on another).  Gathers, the queue reset, the
-// persistent kernel and the cross-split reductions are captured once into a
-// CUDA graph; holo_batch_execute replays it.
+// one transform_full per plane.  Here every problem is planned once (tile
+// shape and pair model as for a single transform); problems whose plans chose
+// the same kernel variant form a group, whose (target tile, source range) work
+// items go into one device work queue sorted longest-first, drained by one
+// persistent split-precision kernel with an atomic counter (no CTA waits on
+// another).  Gathers, the queue reset, one queue kernel per group and the
+// cross-split reductions are captured once into a CUDA graph;
+// holo_batch_execute replays it.
 #include <algorithm>
 #include <memory>
 
@@ -16,121 +18,136 @@ using namespace holo;
 
 namespace {
 
-struct BatchState {
-  std::vector<SplitProblem> probs;     // host copies of the descriptors
-  std::vector<double2 *> ap;           // per-problem gathered (phase, amp)
-  std::vector<const double *> amp, phase;
-  SplitProblem *probs_dev = nullptr;
-  WorkItem *items_dev = nullptr;
-  int *queue = nullptr;
-  int *offsets_dev = nullptr;
-  int n_items = 0;
-  int total_targets = 0;
+// Problems whose plans chose the same kernel variant share one persistent
+// queue kernel; each group has its own work items and queue counter.
+struct Group {
   int variant = 0;
+  std::vector<WorkItem> items;
+  WorkItem *items_dev = nullptr;
   int grid = 0;
 };
 
+// The split-precision descriptor of problem i with its source range cut into
+// `splits` parts; its work items go to `items`.
+int describe_problem(holo_batch_s *b, const holo_problem &q, holo_plan_s *p, int i, int splits,
+                     SplitProblem *P, std::vector<WorkItem> *items, cudaStream_t s) {
+  holo_handle h = b->h;
+  p->splits = splits;
+  *P = SplitProblem{};
+  P->pos_s = p->pos_s;
+  P->geo_s = p->geo_s;
+  P->geo_t = p->geo_t;
+  P->tiles_s = p->tiles_s;
+  P->pos_t = p->pos_t;
+  P->tiles_t = p->tiles_t;
+  P->order_t = p->order_t;
+  P->y = (double2 *)q.y_re_im;
+  P->N = p->N;
+  P->M = p->M;
+  P->n_stiles = p->n_stiles;
+  P->n_ttiles = p->n_ttiles;
+  P->splits = splits;
+  P->sign = q.sign;
+  P->sk = q.sign * ((2.0 * M_PI) / q.lambda);
+  P->sub = 1;
+  float2 *apf = (float2 *)pool_alloc(h, (size_t)p->n_pad * sizeof(float2), s);
+  if (!apf) return fail(HOLO_ERR_ALLOC, "batch gather buffer");
+  b->owned.push_back(apf);
+  P->apf_s = apf;
+  if (splits > 1) {
+    double2 *part = (double2 *)pool_alloc(h, (size_t)splits * p->M * sizeof(double2), s);
+    if (!part) return fail(HOLO_ERR_ALLOC, "batch partial buffer");
+    b->owned.push_back(part);
+    P->partial = part;
+  }
+  for (int t = 0; t < p->n_ttiles; ++t)
+    for (int sp = 0; sp < splits; ++sp) {
+      WorkItem w{};
+      w.problem = i;
+      w.ttile = t;
+      w.split = sp;
+      w.s_begin = (int)(((long long)p->n_stiles * sp) / splits);
+      w.s_end = (int)(((long long)p->n_stiles * (sp + 1)) / splits);
+      if (p->N > 0 && w.s_end > w.s_begin) items->push_back(w);
+    }
+  return HOLO_OK;
+}
+
 int batch_build(holo_batch_s *b, const holo_problem *pr, int n, int precision, cudaStream_t s) {
   holo_handle h = b->h;
-  BatchState st;
-  // FP64 batches are captured as a sequence of per-problem launches.
-  const bool split = precision == HOLO_SPLIT32;
-  st.variant = 9;  // the default variant for target sets of 1024 and more
-  const Variant V = split ? split_variant(st.variant) : fp64_variant(0);
-  int occ = 1;
-  if (split) HOLO_TRY(split_occupancy(st.variant, false, &occ));
-  const int G = std::max(1, occ) * h->sm_count;
-
-  long long work = 0;  // tile pairs
+  // every problem planned on its own: tile shape and pair model as for a
+  // single transform of it (FP64 batches are captured by the caller as a
+  // sequence of per-problem launches)
   for (int i = 0; i < n; ++i) {
     holo_plan_s *p = nullptr;
-    HOLO_TRY(plan_create_impl(h, pr[i].u_xyz, pr[i].N, pr[i].v_xyz, pr[i].M, precision,
-                              split ? st.variant : -1, s, &p));
+    HOLO_TRY(plan_create_impl(h, pr[i].u_xyz, pr[i].N, pr[i].v_xyz, pr[i].M, precision, -1, s,
+                              &p));
     b->plans.push_back(p);
-    work += (long long)p->n_ttiles * p->n_stiles;
     b->total_pairs += (long long)pr[i].N * (long long)pr[i].M;
   }
-  if (!split) return HOLO_OK;
+  if (precision != HOLO_SPLIT32) return HOLO_OK;
 
-  // split every problem's source range so that items are ~1/8 of a CTA's share
-  const double target_item = std::max(1.0, (double)work / ((double)G * 8.0));
-  std::vector<WorkItem> items;
-  std::vector<int> offsets(n + 1, 0);
-  st.probs.resize(n);
+  std::vector<Group> groups;
+  std::vector<int> group_of(n);
   for (int i = 0; i < n; ++i) {
-    holo_plan_s *p = b->plans[i];
-    int splits = (int)std::min<double>(p->n_stiles, std::max(1.0, ceil(p->n_stiles / target_item)));
-    splits = std::max(1, std::min(splits, (int)std::max<size_t>(1, ((size_t)1 << 28) / std::max(p->M, 1))));
-    p->splits = splits;
-    SplitProblem &P = st.probs[i];
-    P = SplitProblem{};
-    P.pos_s = p->pos_s;
-    P.geo_s = p->geo_s;
-    P.geo_t = p->geo_t;
-    P.tiles_s = p->tiles_s;
-    P.pos_t = p->pos_t;
-    P.tiles_t = p->tiles_t;
-    P.order_t = p->order_t;
-    P.y = (double2 *)pr[i].y_re_im;
-    P.N = p->N;
-    P.M = p->M;
-    P.n_stiles = p->n_stiles;
-    P.n_ttiles = p->n_ttiles;
-    P.splits = splits;
-    P.sign = pr[i].sign;
-    P.sk = pr[i].sign * ((2.0 * M_PI) / pr[i].lambda);
-    P.sub = 1;
-    double2 *ap = (double2 *)pool_alloc(h, (size_t)p->n_pad * sizeof(double2), s);
-    if (!ap) return fail(HOLO_ERR_ALLOC, "batch gather buffer");
-    b->owned.push_back(ap);
-    P.apf_s = reinterpret_cast<float2 *>(ap);
-    if (splits > 1) {
-      double2 *part = (double2 *)pool_alloc(h, (size_t)splits * p->M * sizeof(double2), s);
-      if (!part) return fail(HOLO_ERR_ALLOC, "batch partial buffer");
-      b->owned.push_back(part);
-      P.partial = part;
+    size_t g = 0;
+    while (g < groups.size() && groups[g].variant != b->plans[i]->variant) ++g;
+    if (g == groups.size()) {
+      groups.emplace_back();
+      groups.back().variant = b->plans[i]->variant;
     }
-    for (int t = 0; t < p->n_ttiles; ++t)
-      for (int sp = 0; sp < splits; ++sp) {
-        WorkItem w{};
-        w.problem = i;
-        w.ttile = t;
-        w.split = sp;
-        w.s_begin = (int)(((long long)p->n_stiles * sp) / splits);
-        w.s_end = (int)(((long long)p->n_stiles * (sp + 1)) / splits);
-        if (p->N > 0 && w.s_end > w.s_begin) items.push_back(w);
-      }
-    offsets[i + 1] = offsets[i] + p->M;
+    group_of[i] = (int)g;
   }
-  // longest items first: the atomic queue then approximates LPT scheduling
-  std::stable_sort(items.begin(), items.end(), [&](const WorkItem &a, const WorkItem &c) {
-    const long long ca = (long long)(a.s_end - a.s_begin);
-    const long long cc = (long long)(c.s_end - c.s_begin);
-    return ca > cc;
-  });
-  st.n_items = (int)items.size();
-  st.total_targets = offsets[n];
-  st.grid = std::max(1, std::min(G, st.n_items));
-  st.probs_dev = (SplitProblem *)pool_alloc(h, sizeof(SplitProblem) * std::max(n, 1), s);
-  st.items_dev = (WorkItem *)pool_alloc(h, sizeof(WorkItem) * std::max<size_t>(items.size(), 1), s);
-  st.queue = (int *)pool_alloc(h, sizeof(int), s);
-  st.offsets_dev = (int *)pool_alloc(h, sizeof(int) * (n + 1), s);
-  if (!st.probs_dev || !st.items_dev || !st.queue || !st.offsets_dev)
-    return fail(HOLO_ERR_ALLOC, "batch descriptors");
-  b->owned.push_back(st.probs_dev);
-  b->owned.push_back(st.items_dev);
-  b->owned.push_back(st.queue);
-  b->owned.push_back(st.offsets_dev);
-  HOLO_CUDA(cudaMemcpyAsync(st.probs_dev, st.probs.data(), sizeof(SplitProblem) * n,
-                            cudaMemcpyHostToDevice, s));
-  if (!items.empty())
-    HOLO_CUDA(cudaMemcpyAsync(st.items_dev, items.data(), sizeof(WorkItem) * items.size(),
+  std::vector<SplitProblem> probs(n);
+  std::vector<int> offsets(n + 1, 0);
+  for (int i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + b->plans[i]->M;
+  for (size_t g = 0; g < groups.size(); ++g) {
+    Group &G = groups[g];
+    int occ = 1;
+    HOLO_TRY(split_occupancy(G.variant, false, &occ));
+    const int slots = std::max(1, occ) * h->sm_count;
+    long long work = 0;  // tile pairs of the group
+    for (int i = 0; i < n; ++i)
+      if (group_of[i] == (int)g) work += (long long)b->plans[i]->n_ttiles * b->plans[i]->n_stiles;
+    // split every problem's source range so that items are ~1/8 of a CTA's share
+    const double target_item = std::max(1.0, (double)work / ((double)slots * 8.0));
+    for (int i = 0; i < n; ++i) {
+      if (group_of[i] != (int)g) continue;
+      holo_plan_s *p = b->plans[i];
+      int splits = (int)std::min<double>(p->n_stiles, std::max(1.0, ceil(p->n_stiles / target_item)));
+      splits = std::max(1, std::min(splits, (int)std::max<size_t>(1, ((size_t)1 << 28) / std::max(p->M, 1))));
+      HOLO_TRY(describe_problem(b, pr[i], p, i, splits, &probs[i], &G.items, s));
+    }
+    // longest items first: the atomic queue then approximates LPT scheduling
+    std::stable_sort(G.items.begin(), G.items.end(), [](const WorkItem &x, const WorkItem &y) {
+      return x.s_end - x.s_begin > y.s_end - y.s_begin;
+    });
+    G.grid = std::max(1, std::min(slots, (int)G.items.size()));
+  }
+  const int ng = (int)groups.size();
+  SplitProblem *probs_dev = (SplitProblem *)pool_alloc(h, sizeof(SplitProblem) * std::max(n, 1), s);
+  int *queues = (int *)pool_alloc(h, sizeof(int) * std::max(ng, 1), s);
+  int *offsets_dev = (int *)pool_alloc(h, sizeof(int) * (n + 1), s);
+  if (!probs_dev || !queues || !offsets_dev) return fail(HOLO_ERR_ALLOC, "batch descriptors");
+  b->owned.push_back(probs_dev);
+  b->owned.push_back(queues);
+  b->owned.push_back(offsets_dev);
+  for (Group &G : groups) {
+    G.items_dev = (WorkItem *)pool_alloc(h, sizeof(WorkItem) * std::max<size_t>(G.items.size(), 1), s);
+    if (!G.items_dev) return fail(HOLO_ERR_ALLOC, "batch work items");
+    b->owned.push_back(G.items_dev);
+    if (!G.items.empty())
+      HOLO_CUDA(cudaMemcpyAsync(G.items_dev, G.items.data(), sizeof(WorkItem) * G.items.size(),
+                                cudaMemcpyHostToDevice, s));
+  }
+  if (n > 0)
+    HOLO_CUDA(cudaMemcpyAsync(probs_dev, probs.data(), sizeof(SplitProblem) * n,
                               cudaMemcpyHostToDevice, s));
-  HOLO_CUDA(cudaMemcpyAsync(st.offsets_dev, offsets.data(), sizeof(int) * (n + 1),
+  HOLO_CUDA(cudaMemcpyAsync(offsets_dev, offsets.data(), sizeof(int) * (n + 1),
                             cudaMemcpyHostToDevice, s));
   HOLO_CUDA(cudaStreamSynchronize(s));  // host vectors above are about to go away
 
-  // ---- capture the graph ----
+  // ---- capture the graph: gathers, queue reset, one queue kernel per group, reductions ----
   cudaStream_t cap;
   HOLO_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
   int rc = HOLO_OK;
@@ -141,14 +158,14 @@ int batch_build(holo_batch_s *b, const holo_problem *pr, int n, int precision, c
   }
   for (int i = 0; i < n && rc == HOLO_OK; ++i)
     rc = launch_gather_apf(pr[i].amp, pr[i].phase, b->plans[i]->order_s, b->plans[i]->N,
-                          b->plans[i]->n_pad, const_cast<float2 *>(st.probs[i].apf_s), cap);
-  if (rc == HOLO_OK && cudaMemsetAsync(st.queue, 0, sizeof(int), cap) != cudaSuccess)
+                           b->plans[i]->n_pad, const_cast<float2 *>(probs[i].apf_s), cap);
+  if (rc == HOLO_OK && ng > 0 && cudaMemsetAsync(queues, 0, sizeof(int) * ng, cap) != cudaSuccess)
     rc = fail(HOLO_ERR_CUDA, "queue reset during capture");
-  if (rc == HOLO_OK && st.n_items > 0)
-    rc = launch_split_batched(st.probs_dev, st.items_dev, st.n_items, st.queue, st.variant,
-                              st.grid, h->dev_err, cap);
-  if (rc == HOLO_OK)
-    rc = launch_reduce_batched(st.probs_dev, st.offsets_dev, n, st.total_targets, cap);
+  for (int g = 0; g < ng && rc == HOLO_OK; ++g)
+    if (!groups[g].items.empty())
+      rc = launch_split_batched(probs_dev, groups[g].items_dev, (int)groups[g].items.size(),
+                                queues + g, groups[g].variant, groups[g].grid, h->dev_err, cap);
+  if (rc == HOLO_OK) rc = launch_reduce_batched(probs_dev, offsets_dev, n, offsets[n], cap);
   cudaGraph_t graph = nullptr;
   e = cudaStreamEndCapture(cap, &graph);
   cudaStreamDestroy(cap);
@@ -159,7 +176,6 @@ int batch_build(holo_batch_s *b, const holo_problem *pr, int n, int precision, c
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
   b->graph = graph;
   HOLO_CUDA(cudaGraphInstantiate(&b->exec, graph, 0));
-  (void)V;
   return HOLO_OK;
 }
 

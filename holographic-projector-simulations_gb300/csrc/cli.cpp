@@ -8,7 +8,9 @@
 // (cuda/main.cu:213-221).  Unlike the reference, -F projects z from the
 // normalised projector field y at v onto w (the x -> y -> z chain); --ref-compat
 // reproduces the reference's -F (z from x at u onto v, cuda/main.cu:219).
-// Without -f the generated-data mode of cuda/main.cu:120-199 runs.
+// Without -f the generated-data mode of cuda/main.cu:120-199 runs; the -Z
+// projection planes of one object plane run there as one batched launch
+// (holo_transform_batched) instead of one pass per plane.
 //
 // Long options added here: --lambda, --precision fp64|split32, --mc SUB,
 // --seed S, --mc-block B, --amplitude-only (PROJECT_PHASE=0), --reference-distance,
@@ -16,6 +18,7 @@
 //
 // Exit codes: 0 success; 2 bad arguments or files; 4 non-finite output (the
 // reference's check_complex exit, cuda/util.h:54-60); 3 a library error.
+#include <cuda_runtime.h>
 #include <curand.h>
 #include <getopt.h>
 #include <math.h>
@@ -337,6 +340,76 @@ struct Runner {
     }
     return 0;
   }
+
+  // Forward passes from one source set to several target planes (the
+  // projection planes of -Z): one batched launch over all planes, then each
+  // plane normalised to polar.  *dt is the time of the whole stack.
+  int stack(const std::vector<double> &amp, const std::vector<double> &phase,
+            const std::vector<double> &u, const std::vector<std::vector<double>> &ws,
+            std::vector<std::vector<double>> *oa, std::vector<std::vector<double>> *op,
+            double *dt) {
+    const size_t N = amp.size(), P = ws.size();
+    std::vector<void *> bufs;
+    bool ok = true;
+    auto dev = [&](const double *src, size_t n) -> double * {
+      void *d = nullptr;
+      if (cudaMalloc(&d, (n ? n : 1) * sizeof(double)) != cudaSuccess) {
+        ok = false;
+        return nullptr;
+      }
+      bufs.push_back(d);
+      if (src && n && cudaMemcpy(d, src, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+        ok = false;
+      return static_cast<double *>(d);
+    };
+    auto release = [&]() {
+      for (void *d : bufs) cudaFree(d);
+    };
+    const double t0 = now();
+    double *da = dev(amp.data(), N), *dp = dev(phase.data(), N), *du = dev(u.data(), 3 * N);
+    std::vector<holo_problem> probs(P);
+    for (size_t j = 0; j < P && ok; ++j) {
+      const size_t M = ws[j].size() / 3;
+      double *dw = dev(ws[j].data(), 3 * M), *dz = dev(nullptr, 2 * M);
+      probs[j] = holo_problem{da, dp, du, N, dw, M, HOLO_FORWARDS, p.lambda, dz};
+    }
+    if (!ok) {
+      release();
+      fprintf(stderr, "holo: device buffers for the plane stack: %s\n",
+              cudaGetErrorString(cudaGetLastError()));
+      return 3;
+    }
+    int rc = holo_transform_batched(h, probs.data(), (int)P, p.precision, nullptr);
+    if (rc) {
+      release();
+      return lib_fail("holo_transform_batched", rc);
+    }
+    oa->assign(P, {});
+    op->assign(P, {});
+    for (size_t j = 0; j < P && rc == 0; ++j) {
+      const size_t M = probs[j].M;
+      std::vector<double> z(2 * M);
+      if (cudaMemcpy(z.data(), probs[j].y_re_im, 2 * M * sizeof(double),
+                     cudaMemcpyDeviceToHost) != cudaSuccess) {
+        fprintf(stderr, "holo: copy of plane %zu failed\n", j);
+        rc = 3;
+        break;
+      }
+      (*oa)[j].assign(M, 0.0);
+      (*op)[j].assign(M, 0.0);
+      rc = holo_normalize_polar(h, z.data(), M, (*oa)[j].data(), (*op)[j].data(), nullptr,
+                                nullptr);
+      if (rc) {
+        rc = lib_fail("holo_normalize_polar", rc);
+      } else if (!finite_all((*oa)[j]) || !finite_all((*op)[j])) {
+        fprintf(stderr, "holo: non-finite output\n");
+        rc = 4;
+      }
+    }
+    *dt = now() - t0;
+    release();
+    return rc;
+  }
 };
 
 int write(const std::vector<double> &a, const std::vector<double> &ph,
@@ -435,6 +508,10 @@ int generated_mode(Runner &R, const Params &p) {
     if ((rc = write(ya, yp, v, "y" + xs, "v" + xs, y_plane, dt, flops(dt, xa.size(), ya.size()),
                     p.out_dir)))
       return rc;
+    // the projection planes (-Z) share the sources y: with more than one they
+    // run as one batched launch (Monte Carlo sampling keeps one pass each)
+    std::vector<std::vector<double>> ws;
+    std::vector<holo_io::Plane> zpl;
     for (size_t j = 0; j < p.planes_projection; ++j) {
       const double r2 = j == 0 ? 0.0 : j / ((double)p.planes_projection - 1.);
       const double width = gerp(p.projection_width, r2), height = width / p.aspect_projection;
@@ -445,11 +522,27 @@ int generated_mode(Runner &R, const Params &p) {
                              p.aspect_projection,
                              p.randomize};
       if (!lattice(w, z_plane)) return lib_fail("cuRAND", -2);
+      ws.push_back(w);
+      zpl.push_back(z_plane);
+    }
+    const bool batched = ws.size() > 1 && p.mc_sub == 0;
+    std::vector<std::vector<double>> zas, zps;
+    double dt_plane = 0.0;
+    if (batched) {
+      if ((rc = R.stack(ya, yp, v, ws, &zas, &zps, &dt))) return rc;
+      dt_plane = dt / (double)ws.size();
+    }
+    for (size_t j = 0; j < ws.size(); ++j) {
       std::vector<double> za, zp;
-      if ((rc = R.pass(HOLO_FORWARDS, ya, yp, v, w, &za, &zp, &dt, false))) return rc;
+      if (batched) {
+        za.swap(zas[j]);
+        zp.swap(zps[j]);
+      } else {
+        if ((rc = R.pass(HOLO_FORWARDS, ya, yp, v, ws[j], &za, &zp, &dt_plane, false))) return rc;
+      }
       const std::string zs = xs + "_" + std::to_string(j);
-      if ((rc = write(za, zp, w, "z" + zs, "w" + zs, z_plane, dt,
-                      flops(dt, ya.size(), za.size()), p.out_dir)))
+      if ((rc = write(za, zp, ws[j], "z" + zs, "w" + zs, zpl[j], dt_plane,
+                      flops(dt_plane, ya.size(), za.size()), p.out_dir)))
         return rc;
     }
   }

@@ -91,6 +91,8 @@ struct TileStats {
 //         400 nm) of the same size.
 // Infinite when the two point sets' boxes touch.
 void split_error_model(const TileStats &st, double *base, double *curv, double *lin);
+// Path-length error budget of the split path: 5e-6 rad at lambda = 400 nm.
+constexpr double kSplitBoundMetres = 5e-6 * 400e-9 / (2.0 * 3.14159265358979323846);
 int fp64_variant_count();
 Variant fp64_variant(int i);
 
@@ -214,6 +216,7 @@ struct holo_plan_s {
   int grid = 0;
   int n_stiles = 0, n_ttiles = 0;
   double err_bound = 0.0;        // split path: bound on the path-length error (m)
+  double model_bounds[3] = {0.0, 0.0, 0.0};  // the same for pair models 0, 1, 2 (same tiles)
   cudaStream_t last_stream = nullptr;
   // device buffers
   double *pos_s = nullptr;       // 3 * n_pad

@@ -192,7 +192,7 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
 
   // ---- tile size: the largest whose path-length error bound holds ----
   const int cands[] = {9, 11, 3, 4};
-  const double budget = 5e-6 * 400e-9 / (2.0 * M_PI);
+  const double budget = kSplitBoundMetres;
   int variant = cands[0];
   for (int i = 0; i < 4; ++i) {
     if (M < 1024 && (cands[i] == 9 || cands[i] == 11)) continue;
