@@ -8,8 +8,9 @@ pitch, z = 0.35 m, Gaussian-blob amplitudes, uniform phases, seed 0) through a
 
   value     pair-evals/s with inputs resident in HBM (holo_project on device buffers)
   e2e       the same through the C ABI with host buffers (copies inside the timing)
-  roofline  the pair kernel's MUFU (XU pipe) issue rate, 3 MUFU ops per pair,
-            against this GPU's MUFU rate measured by holo_probe_peak
+  roofline  the pair kernel's lane-op rate on its busier pipe (FP32 FMA or XU/MUFU;
+            ops per pair from the planned variant's pair model and sin/cos split)
+            against that pipe's rate on this GPU measured by holo_probe_peak
   cpu_baseline  the C oracle (FP64, all host threads) on a bounded target sample
 
 ``--impl reference`` times the reference's own CPU algorithm for this path --
@@ -222,6 +223,17 @@ def run_profile_case(args):
         print(json.dumps({"profile_case": pl.info(), "pairs_per_launch": len(amp) * len(vv)}))
 
 
+def mc_expected_rel_l2(amp, u, v, y, sub, n_sample=256, seed=7):
+    """Expected rel-L2 of stratified sampling (one source drawn per stratum of `sub`,
+    weight `sub`) for sources with independent uniform phases: the error variance per
+    target is (sub - 1) sum_n |a_n / r_n|^2, so rel-L2 ~ sqrt((sub - 1) sum_mn
+    |a_n / r_mn|^2) / |y|; sum_mn taken from `n_sample` random targets."""
+    idx = np.random.default_rng(seed).choice(len(v), size=min(n_sample, len(v)), replace=False)
+    d2 = ((v[idx, None, :] - u[None, :, :]) ** 2).sum(-1)
+    power = float((amp[None, :] ** 2 / d2).sum()) * len(v) / len(idx)
+    return float(np.sqrt((sub - 1) * power) / np.linalg.norm(y))
+
+
 def _events_ms(fn, reps=1):
     import torch
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -276,6 +288,7 @@ def run_other_workload(args):
                 "sampled_pair_evals_per_s": len(u) // 16 * len(v) / (ms * 1e-3),
                 "effective_pair_evals_per_s": len(u) * len(v) / (ms * 1e-3),
                 "mc_rel_l2_vs_fp64": float(np.linalg.norm(ymc - y64) / np.linalg.norm(y64)),
+                "mc_expected_rel_l2": mc_expected_rel_l2(amp, u, v, y64, 16),
                 "config": "x->y pass of config 1, 1/16 of the sources per block of 256 targets"})
     elif args.workload == "config4":
         probs, pairs = [], 0
@@ -460,7 +473,7 @@ def main():
     h2d = 8 * (2 * N + 3 * N + 3 * M + 3 * P)
     d2h = 8 * (2 * M + 2 * P)
 
-    # roofline of the pair kernel: MUFU (XU pipe) issue rate against the measured peak
+    # roofline of the pair kernel: FP32 and MUFU (XU pipe) issue rates against measured peaks
     kern_pairs_s = pairs_step * args.steps / (kern_ms * 1e-3) if kern_ms > 0 else 0.0
     mufu_peak = h.probe_peak(0)
     ffma_peak = h.probe_peak(1)
@@ -478,15 +491,26 @@ def main():
         except (OSError, ValueError):
             traffic = None
     # the pair rate this variant could reach if its busiest pipe ran at the measured peak
-    bound_rate = min(mufu_peak / MUFU_PER_PAIR, ffma_peak / FP32_PER_PAIR) if var else None
-    roofline = {"bound": "xu", "achieved": achieved / 1e9, "peak": mufu_peak / 1e9,
-                "unit": "Gop/s", "frac": achieved / mufu_peak if mufu_peak else None,
+    bound_rate = min(mufu_peak / MUFU_PER_PAIR if MUFU_PER_PAIR else float("inf"),
+                     ffma_peak / FP32_PER_PAIR if FP32_PER_PAIR else float("inf")) if var else None
+    # the bound named is the busier of the two pipes (FP32 FMA pipe, XU/MUFU pipe)
+    fp32_ops = kern_pairs_s * FP32_PER_PAIR
+    xu_frac = achieved / mufu_peak if mufu_peak else 0.0
+    fp32_frac = fp32_ops / ffma_peak if ffma_peak else 0.0
+    busy_fp32 = fp32_frac > xu_frac
+    roofline = {"bound": "fp32" if busy_fp32 else "xu",
+                "achieved": (fp32_ops if busy_fp32 else achieved) / 1e9,
+                "peak": (ffma_peak if busy_fp32 else mufu_peak) / 1e9,
+                "unit": "Gop/s", "frac": fp32_frac if busy_fp32 else xu_frac,
                 "traffic": traffic,
-                "note": "compute-bound: MUFU (XU pipe) ops of the pair kernel per second vs the "
-                        "MUFU rate measured by holo_probe_peak (sin.approx throughput); neither "
-                        "HBM nor tensor cores bound this path",
+                "note": "compute-bound on the FP32 (FMA) and XU (MUFU) pipes: the busier pipe's "
+                        "lane-ops of the pair kernel per second vs that pipe's rate measured by "
+                        "holo_probe_peak (FFMA / sin.approx throughput kernels); neither HBM nor "
+                        "tensor cores bound this path",
+                "xu_frac": xu_frac, "xu_achieved_gops": achieved / 1e9,
+                "xu_peak_gops": mufu_peak / 1e9,
                 "variant": var, "mufu_per_pair": MUFU_PER_PAIR, "fp32_per_pair": FP32_PER_PAIR,
-                "fp32_frac": kern_pairs_s * FP32_PER_PAIR / ffma_peak if ffma_peak else None,
+                "fp32_frac": fp32_frac,
                 "fma_peak_gops": ffma_peak / 1e9,
                 "pairs_per_s_frac_of_pipe_bound": kern_pairs_s / bound_rate if bound_rate else None,
                 "kernel_pairs_per_s": kern_pairs_s,
