@@ -41,8 +41,11 @@ def pipe_ops_per_pair(variant: dict) -> tuple[float, float]:
     0 (curvature correction): 3 MUFU (rsqrt, sin, cos) + 12 FP32; 1 (without it):
     3 + 10; 2 (1/q series, no rsqrt): 2 + 8.  `fma_sincos_targets` of every
     `targets_per_thread` take sin/cos from the FMA-pipe polynomial instead
-    (+16 FP32, -2 MUFU)."""
+    (+16 FP32, -2 MUFU); with warp-specialised sin/cos (pair loop 2) a quarter of the
+    warps do."""
     f = variant["fma_sincos_targets"] / variant["targets_per_thread"]
+    if variant.get("pair_loop", 0) == 2:
+        f = 0.25
     mufu, fp32 = {0: (3.0, 12.0), 1: (3.0, 10.0), 2: (2.0, 8.0)}[variant.get("pair_model", 0)]
     return mufu - 2.0 * f, fp32 + 16.0 * f
 
@@ -354,7 +357,10 @@ def run_sweep(args):
     d = [t(a) for a in (amp, phase, u, v)]
     h = holo.handle(0)
     ref = None
+    only = {int(x) for x in args.variants.split(",")} if args.variants else None
     for var in holo.variants("split32"):
+        if only is not None and var["variant"] not in only:
+            continue
         try:
             holo.transform(*d, -1, LAM, precision="split32", variant=var["variant"])
             torch.cuda.synchronize()
@@ -385,6 +391,8 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: two split-FP32 passes of the 512^2 sources onto "
                          "a 256^2 patch of the projector (1.7e10 pairs each), then exit")
+    ap.add_argument("--variants", default="",
+                    help="comma-separated variant numbers to restrict --sweep-variants to")
     ap.add_argument("--sweep-variants", action="store_true",
                     help="time every split-FP32 kernel variant on the config-2 y pass, then exit")
     ap.add_argument("--workload", default="config2",

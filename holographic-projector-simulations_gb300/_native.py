@@ -71,7 +71,7 @@ SIGNATURES = {
     "holo_transform_batched": (_i, [_vp, _c.POINTER(HoloProblem), _i, _i, _vp]),
     "holo_variant_count": (_i, [_i]),
     "holo_variant_describe": (_i, [_i, _i, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i),
-                                   _c.POINTER(_i), _c.POINTER(_i)]),
+                                   _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)]),
     "holo_set_variant": (_i, [_vp, _i, _i, _i]),
     "holo_get_variant": (_i, [_vp, _i, _i, _c.POINTER(_i)]),
     "holo_size_bucket": (_i, [_sz, _sz]),

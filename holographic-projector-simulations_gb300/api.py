@@ -419,12 +419,13 @@ def variants(precision="split32") -> list[dict]:
     pr = _precision(precision)
     out = []
     for i in range(L.holo_variant_count(pr)):
-        t, r, c, q, k = (ctypes.c_int() for _ in range(5))
+        t, r, c, q, k, lp = (ctypes.c_int() for _ in range(6))
         N.check(L.holo_variant_describe(pr, i, ctypes.byref(t), ctypes.byref(r), ctypes.byref(c),
-                                        ctypes.byref(q), ctypes.byref(k)))
+                                        ctypes.byref(q), ctypes.byref(k), ctypes.byref(lp)))
         out.append({"variant": i, "threads": t.value, "targets_per_thread": r.value,
                     "source_tile": c.value, "target_tile": t.value * r.value,
-                    "fma_sincos_targets": q.value, "pair_model": k.value})
+                    "fma_sincos_targets": q.value, "pair_model": k.value,
+                    "pair_loop": lp.value})
     return out
 
 

@@ -1022,7 +1022,8 @@ int holo_variant_count(int precision) {
 }
 
 int holo_variant_describe(int precision, int variant, int *threads, int *targets_per_thread,
-                          int *source_tile, int *fma_sincos_targets, int *pair_model) {
+                          int *source_tile, int *fma_sincos_targets, int *pair_model,
+                          int *pair_loop) {
   const int n = holo_variant_count(precision);
   if (n < 0) return n;
   if (variant < 0 || variant >= n) return fail(HOLO_ERR_INVALID, "variant %d out of range", variant);
@@ -1032,6 +1033,7 @@ int holo_variant_describe(int precision, int variant, int *threads, int *targets
   if (source_tile) *source_tile = V.cs;
   if (fma_sincos_targets) *fma_sincos_targets = V.poly;
   if (pair_model) *pair_model = V.model;
+  if (pair_loop) *pair_loop = V.ws ? 2 : V.packed;
   return HOLO_OK;
 }
 

@@ -65,6 +65,7 @@ struct Variant {
                  //   2: c / 2q with 1/q to first order in Ps / Qt  (8 FP32 + 2 MUFU)
                  // the planner takes model 1 or 2 only when its error bound allows
   int packed = 0; // 1: pair loop on packed FP32 pairs (two sources per instruction)
+  int ws = 0;     // 1: warp-specialised sin/cos (`poly` is then the average per thread)
   int tt() const { return threads * r; }
 };
 

@@ -193,6 +193,69 @@ __device__ __forceinline__ void poly_sincos2(uint64_t th, uint64_t &sn, uint64_t
   cs = c;
 }
 
+// Pair loop of pair model 2 on packed FP32 pairs: two consecutive sources per
+// instruction for each of the R targets of this thread; the first NP targets
+// take sin/cos from the FMA-pipe polynomial.  Per-target inputs: frame
+// coordinates Tx, Ty, T2 = Tx^2 + Ty^2, Iq = |kap2| / Qt, Kq = |kap2| / Qt^2;
+// outputs the FP32 tile sums (re, im) per target (before the 1 / Qt factor).
+template <int R, int NP, bool CONST>
+__device__ __forceinline__ void packed_pairs(const float4 *pa, const float4 *pb, const float4 *pc,
+                                             int npair, const float *Tx, const float *Ty,
+                                             const float *T2, const float *Iq, const float *Kq,
+                                             float *re, float *im) {
+  uint64_t tx2[R], ty2[R], t22[R], iq2[R], kq2[R], re2[R], im2[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    tx2[r] = ptx::pack2(Tx[r], Tx[r]);
+    ty2[r] = ptx::pack2(Ty[r], Ty[r]);
+    t22[r] = ptx::pack2(T2[r], T2[r]);
+    iq2[r] = ptx::pack2(Iq[r], Iq[r]);
+    kq2[r] = ptx::pack2(Kq[r], Kq[r]);
+    re2[r] = 0ull;
+    im2[r] = 0ull;
+  }
+#pragma unroll 2
+  for (int p = 0; p < npair; ++p) {
+    const float4 c4 = pc[p];
+    if (CONST) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) re[r] += c4.x + c4.y;
+    } else {
+      const float4 a4 = pa[p], b4 = pb[p];
+      const uint64_t qx = ptx::pack2(a4.x, a4.y), qy = ptx::pack2(a4.z, a4.w);
+      const uint64_t qz = ptx::pack2(b4.x, b4.y), qw = ptx::pack2(b4.z, b4.w);
+      const uint64_t am = ptx::pack2(c4.x, c4.y), s2 = ptx::pack2(c4.z, c4.w);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const uint64_t c = ptx::fma2(tx2[r], qx, ptx::fma2(ty2[r], qy, ptx::add2(t22[r], s2)));
+        const uint64_t iq = ptx::fma2(qz, kq2[r], iq2[r]);  // |kap2| / q, first order
+        const uint64_t th = ptx::fma2(c, iq, qw);           // sign * theta
+        uint64_t sn, cs;
+        if (r < NP) {
+          poly_sincos2(th, sn, cs);  // FMA pipe
+        } else {
+          float t0, t1;
+          ptx::unpack2(th, t0, t1);
+          sn = ptx::pack2(ptx::sin_approx(t0), ptx::sin_approx(t1));  // XU pipe
+          cs = ptx::pack2(ptx::cos_approx(t0), ptx::cos_approx(t1));
+        }
+        re2[r] = ptx::fma2(am, cs, re2[r]);
+        im2[r] = ptx::fma2(am, sn, im2[r]);
+      }
+    }
+  }
+  if (!CONST) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      float a, b;
+      ptx::unpack2(re2[r], a, b);
+      re[r] = a + b;
+      ptx::unpack2(im2[r], a, b);
+      im[r] = a + b;
+    }
+  }
+}
+
 // One staging buffer of source records (float-float offsets + (phase, amp)):
 // the bulk copy of tile j+1 is issued once the frame phase of tile j has
 // consumed it, so it overlaps tile j's pair loop.
@@ -265,7 +328,12 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
   constexpr bool LIN = (POLY & 32) != 0;
   constexpr bool CORR = (POLY & 48) == 0;
   constexpr bool PK = (POLY & 64) != 0;
+  // | 128 (packed only): warp-specialised sin/cos -- a quarter of the warps on the
+  // polynomial for all their targets, the rest on the MUFU pipe
+  constexpr bool WS = (POLY & 128) != 0;
   static_assert(!PK || LIN, "packed pair loop: pair model 2 only");
+  static_assert(!WS || (PK && THREADS % 128 == 0 && THREADS >= 512),
+                "warp specialisation: packed, one polynomial warp per sub-partition");
   const float ak = fabsf(kap2), ak2 = kap2 * kap2, iak = 1.f / fabsf(kap2);
   const float sgn = kap2 < 0.f ? -1.f : 1.f;
 
@@ -456,56 +524,15 @@ __device__ __forceinline__ bool process_item(const SplitProblem &P, int tt, int 
       const float4 *pa = reinterpret_cast<const float4 *>(rec), *pb = pa + CS / 2;
       const float4 *pc = reinterpret_cast<const float4 *>(ramp);
       const int npair = (count + 1) >> 1;
-      uint64_t tx2[R], ty2[R], t22[R], iq2[R], kq2[R], re2[R], im2[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        tx2[r] = ptx::pack2(Tx[r], Tx[r]);
-        ty2[r] = ptx::pack2(Ty[r], Ty[r]);
-        t22[r] = ptx::pack2(T2[r], T2[r]);
-        iq2[r] = ptx::pack2(Qt[r], Qt[r]);
-        kq2[r] = ptx::pack2(kq[r], kq[r]);
-        re2[r] = 0ull;
-        im2[r] = 0ull;
-      }
-#pragma unroll 2
-      for (int p = 0; p < npair; ++p) {
-        const float4 c4 = pc[p];
-        if (CONST) {
-#pragma unroll
-          for (int r = 0; r < R; ++r) re[r] += c4.x + c4.y;
-        } else {
-          const float4 a4 = pa[p], b4 = pb[p];
-          const uint64_t qx = ptx::pack2(a4.x, a4.y), qy = ptx::pack2(a4.z, a4.w);
-          const uint64_t qz = ptx::pack2(b4.x, b4.y), qw = ptx::pack2(b4.z, b4.w);
-          const uint64_t am = ptx::pack2(c4.x, c4.y), s2 = ptx::pack2(c4.z, c4.w);
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const uint64_t c = ptx::fma2(tx2[r], qx, ptx::fma2(ty2[r], qy, ptx::add2(t22[r], s2)));
-            const uint64_t iq = ptx::fma2(qz, kq2[r], iq2[r]);  // |kap2| / q, first order
-            const uint64_t th = ptx::fma2(c, iq, qw);           // sign * theta
-            uint64_t sn, cs;
-            if (r < NPOLY) {
-              poly_sincos2(th, sn, cs);  // FMA pipe
-            } else {
-              float t0, t1;
-              ptx::unpack2(th, t0, t1);
-              sn = ptx::pack2(ptx::sin_approx(t0), ptx::sin_approx(t1));  // XU pipe
-              cs = ptx::pack2(ptx::cos_approx(t0), ptx::cos_approx(t1));
-            }
-            re2[r] = ptx::fma2(am, cs, re2[r]);
-            im2[r] = ptx::fma2(am, sn, im2[r]);
-          }
-        }
-      }
-      if (!CONST) {
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          float a, b;
-          ptx::unpack2(re2[r], a, b);
-          re[r] = a + b;
-          ptx::unpack2(im2[r], a, b);
-          im[r] = a + b;
-        }
+      if (WS) {
+        // the last quarter of the warps (one per SM sub-partition) take every
+        // sin/cos from the polynomial, the others from the MUFU pipe
+        if ((tid >> 5) >= (THREADS >> 5) * 3 / 4)
+          packed_pairs<R, R, CONST>(pa, pb, pc, npair, Tx, Ty, T2, Qt, kq, re, im);
+        else
+          packed_pairs<R, 0, CONST>(pa, pb, pc, npair, Tx, Ty, T2, Qt, kq, re, im);
+      } else {
+        packed_pairs<R, NPOLY, CONST>(pa, pb, pc, npair, Tx, Ty, T2, Qt, kq, re, im);
       }
     } else {
 #pragma unroll 2
@@ -671,6 +698,12 @@ constexpr Variant kVariants[] = {
     {256, 4, 1024, 2, 2, 1},  // 24: 2 of 4 targets on the FMA-pipe sin/cos
     {256, 2, 1024, 1, 2, 1},  // 25: TT 512, 1 of 2
     {128, 4, 1024, 1, 2, 1},  // 26: TT 512, 1 of 4
+    {256, 4, 512, 1, 2, 1},   // 27: as 23 with source tiles of 512 (3 CTAs/SM)
+    {256, 4, 512, 0, 2, 1},   // 28: as 22 with source tiles of 512
+    {128, 4, 512, 1, 2, 1},   // 29: TT 512, source tiles of 512 (5 CTAs/SM)
+    {512, 4, 1024, 1, 2, 1},     // 30: as 23 with 512 threads (TT 2048)
+    {512, 4, 1024, 0, 2, 1, 1},  // 31: as 30, warp-specialised sin/cos (4 of 16 warps polynomial)
+    {512, 2, 1024, 0, 2, 1, 1},  // 32: TT 1024 (tiles of 23), warp-specialised sin/cos
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -730,7 +763,7 @@ int split_twin(int v, int model) {
   for (int i = 0; i < kNumVariants; ++i) {
     const Variant &B = kVariants[i];
     if (B.model == model && B.threads == A.threads && B.r == A.r && B.cs == A.cs &&
-        B.poly == A.poly && (best < 0 || B.packed > kVariants[best].packed))
+        B.poly == A.poly && B.ws == A.ws && (best < 0 || B.packed > kVariants[best].packed))
       best = i;  // the packed pair loop where there is one
   }
   return best;
@@ -765,6 +798,12 @@ int split_twin(int v, int model) {
     case 24: return CALL(256, 4, 1024, 2 | 96);           \
     case 25: return CALL(256, 2, 1024, 1 | 96);           \
     case 26: return CALL(128, 4, 1024, 1 | 96);           \
+    case 27: return CALL(256, 4, 512, 1 | 96);            \
+    case 28: return CALL(256, 4, 512, 0 | 96);            \
+    case 29: return CALL(128, 4, 512, 1 | 96);            \
+    case 30: return CALL(512, 4, 1024, 1 | 96);           \
+    case 31: return CALL(512, 4, 1024, 0 | 96 | 128);     \
+    case 32: return CALL(512, 2, 1024, 0 | 96 | 128);     \
     default: return fail(HOLO_ERR_INVALID, "unknown split variant %d", V); \
   }
 

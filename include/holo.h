@@ -197,14 +197,19 @@ int holo_transform_batched(holo_handle h, const holo_problem *problems, int n_pr
  * a HOLO_SPLIT32 variant says how the curvature term and 1/r are formed per
  * pair: 0 = with the curvature correction c^2/8r^3, 1 = without it, 2 = without
  * it and with 1/r replaced by a first-order series of 1/q (no rsqrt); it is 0
- * for every HOLO_FP64 variant.  The planner picks one tile shape per size
+ * for every HOLO_FP64 variant.  The pair loop is 0 for scalar FP32, 1 for
+ * packed FP32 pairs (f32x2, two sources per instruction), 2 for packed pairs
+ * with warp-specialised sin/cos (a quarter of the warps on the FMA-pipe
+ * polynomial for all their targets; fma_sincos_targets is then 0).  The
+ * planner picks one tile shape per size
  * bucket, then the cheapest pair model whose error bound holds for the point
  * sets; holo_autotune times every variant on a synthetic problem of the given
  * size and records the fastest for its bucket.  The Python layer persists the
  * table as JSON. */
 int holo_variant_count(int precision);
 int holo_variant_describe(int precision, int variant, int *threads, int *targets_per_thread,
-                          int *source_tile, int *fma_sincos_targets, int *pair_model);
+                          int *source_tile, int *fma_sincos_targets, int *pair_model,
+                          int *pair_loop);
 int holo_set_variant(holo_handle h, int precision, int bucket, int variant);
 int holo_get_variant(holo_handle h, int precision, int bucket, int *variant);
 int holo_size_bucket(size_t N, size_t M);

@@ -61,7 +61,7 @@ def test_host_side_validation_without_gpu(holo):
         assert lib.holo_last_error_string()
     else:
         lib.holo_destroy(out)
-    assert lib.holo_variant_describe(1, 99, None, None, None, None, None) == -1
+    assert lib.holo_variant_describe(1, 99, None, None, None, None, None, None) == -1
     assert lib.holo_set_variant(None, 1, 0, 0) == -1
 
 
