@@ -491,13 +491,13 @@ def main():
         if args.precision == "split32" else None
     MUFU_PER_PAIR, FP32_PER_PAIR = pipe_ops_per_pair(var) if var else (0.0, 0.0)
     achieved = kern_pairs_s * MUFU_PER_PAIR
+    # DRAM bytes per pair-kernel launch (the y pass) from the committed ncu capture
     traffic = None
-    prof = os.path.join(REPO, "profiles", "split_kernel_traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("bytes_per_launch_config2")
-        except (OSError, ValueError):
-            traffic = None
+    prof = os.path.join(REPO, "profiles", "k_split_traffic_config2.md")
+    if os.path.exists(prof) and args.precision == "split32":
+        for line in open(prof):
+            if line.startswith("bytes_per_launch_y_pass:"):
+                traffic = int(line.split(":")[1])
     # the pair rate this variant could reach if its busiest pipe ran at the measured peak
     bound_rate = min(mufu_peak / MUFU_PER_PAIR if MUFU_PER_PAIR else float("inf"),
                      ffma_peak / FP32_PER_PAIR if FP32_PER_PAIR else float("inf")) if var else None
