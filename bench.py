@@ -39,14 +39,17 @@ FLOP_PER_PAIR = 29   # the reference's FLOP_PER_POINT (cuda/macros.h:71-80)
 def pipe_ops_per_pair(variant: dict) -> tuple[float, float]:
     """(MUFU ops, FP32-pipe ops) per pair of a split-kernel variant, by pair model:
     0 (curvature correction): 3 MUFU (rsqrt, sin, cos) + 12 FP32; 1 (without it):
-    3 + 10; 2 (1/q series, no rsqrt): 2 + 8.  `fma_sincos_targets` of every
+    3 + 10; 2 (1/q series, no rsqrt): 2 + 8; 3 (phase from tensor-core MMAs): 2 + 3.  `fma_sincos_targets` of every
     `targets_per_thread` take sin/cos from the FMA-pipe polynomial instead
     (+16 FP32, -2 MUFU); with warp-specialised sin/cos (pair loop 2) a quarter of the
     warps do."""
     f = variant["fma_sincos_targets"] / variant["targets_per_thread"]
     if variant.get("pair_loop", 0) == 2:
         f = 0.25
-    mufu, fp32 = {0: (3.0, 12.0), 1: (3.0, 10.0), 2: (2.0, 8.0)}[variant.get("pair_model", 0)]
+    if variant.get("pair_loop", 0) == 3:  # tensor-core phase: `fma_sincos_targets` of 8 pairs
+        f = variant["fma_sincos_targets"] / 8.0
+    mufu, fp32 = {0: (3.0, 12.0), 1: (3.0, 10.0), 2: (2.0, 8.0),
+                  3: (2.0, 3.0)}[variant.get("pair_model", 0)]
     return mufu - 2.0 * f, fp32 + 16.0 * f
 
 

@@ -226,9 +226,13 @@ static int sort_set(holo_plan_s *p, const double *pos, int n, int n_pad, double 
 //          plus the relative amplitude error of 1/r ~ (1 + Ps / r0) / Qt,
 //          x^2 + c / 2q^2 + |Ps| h_t / (Qt r0), as the path length of the same
 //          phase at 400 nm.  |Ps| = |e.s'| <= sum_d |e_d| hd_s[d] with
+//   gemm = rho 2^-22: the curvature term of pair model 3 comes from 3xTF32
+//          tensor-core products (each ~2^-22 relative) summed in the FP32
+//          accumulator, taken as 4 more ulps than the FP32 evaluation in base.
 //          |e_d| <= min(1, span_d / gap) (span_d: the largest target-source
 //          coordinate difference along d), and Qt >= gap - h_t.
-void split_error_model(const TileStats &st, double *base, double *curv, double *lin) {
+void split_error_model(const TileStats &st, double *base, double *curv, double *lin,
+                       double *gemm) {
   double gap2 = 0.0, ps = 0.0;
   for (int d = 0; d < 3; ++d) {
     const double g = std::max(0.0, std::max(st.lo_s[d] - st.hi_t[d], st.lo_t[d] - st.hi_s[d]));
@@ -236,7 +240,7 @@ void split_error_model(const TileStats &st, double *base, double *curv, double *
   }
   const double gap = sqrt(gap2);
   if (!(gap > 0.0)) {
-    *base = *curv = *lin = INFINITY;
+    *base = *curv = *lin = *gemm = INFINITY;
     return;
   }
   for (int d = 0; d < 3; ++d) {
@@ -246,6 +250,7 @@ void split_error_model(const TileStats &st, double *base, double *curv, double *
   const double c = (st.h_s + st.h_t) * (st.h_s + st.h_t), rho = c / (2.0 * gap), y = c / gap2;
   *base = rho * ldexp(1.0, -21) + c / gap * ldexp(1.0, -24) + rho * y * y / 8.0;
   *curv = rho * y / 4.0;
+  *gemm = rho * ldexp(1.0, -22);
   const double qt = gap - st.h_t, x = qt > 0.0 ? ps / qt : INFINITY;
   if (!(x < 0.5)) {
     *lin = INFINITY;
@@ -258,12 +263,12 @@ void split_error_model(const TileStats &st, double *base, double *curv, double *
 // Tile boxes for source tiles of `cs` and target tiles of `tt` points, and the
 // split-path error model of that tiling.
 static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, double *curv,
-                            double *lin, cudaStream_t s) {
+                            double *lin, double *gemm, cudaStream_t s) {
   const int ns = (p->N + cs - 1) / cs, nt = (p->M + tt - 1) / tt;
   HOLO_TRY(launch_tile_bbox(p->pos_s, p->N, cs, p->tiles_s, s));
   HOLO_TRY(launch_tile_bbox(p->pos_t, p->M, tt, p->tiles_t, s));
   if (ns == 0 || nt == 0) {
-    *bound = *curv = *lin = 0.0;
+    *bound = *curv = *lin = *gemm = 0.0;
     return HOLO_OK;
   }
   std::vector<double> ts((size_t)6 * ns), tg((size_t)6 * nt);
@@ -289,7 +294,7 @@ static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, doubl
   TileStats st;
   boxes(ts, ns, st.lo_s, st.hi_s, &st.h_s, st.hd_s);
   boxes(tg, nt, st.lo_t, st.hi_t, &st.h_t, st.hd_t);
-  split_error_model(st, bound, curv, lin);
+  split_error_model(st, bound, curv, lin, gemm);
   return HOLO_OK;
 }
 
@@ -320,34 +325,35 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
     HOLO_TRY(sort_set(p.get(), v, (int)M, (int)M, &p->pos_t, &p->order_t, s));
     HOLO_TRY(alloc_plan(p.get(), (void **)&p->tiles_s, (size_t)6 * (N / 256 + 1) * sizeof(double), s));
     HOLO_TRY(alloc_plan(p.get(), (void **)&p->tiles_t, (size_t)6 * (M / 256 + 1) * sizeof(double), s));
-    // candidates: the chosen variant, then ever smaller tiles until the
-    // path-length error bound holds (sparse or wide point sets need small tiles)
-    std::vector<int> cands = {variant};
-    if (forced_variant < 0)
-      for (int c : {9, 11, 3, 4})
-        if (split_variant(c).tt() < split_variant(variant).tt() ||
-            (split_variant(c).tt() == split_variant(variant).tt() &&
-             split_variant(c).cs < split_variant(variant).cs))
-          cands.push_back(c);
+    // candidates: a forced variant alone; else the variant tuned for this size
+    // bucket, then the preference list (fastest first, ever smaller tiles); the
+    // first whose path-length error bound holds is taken (sparse, wide or close
+    // point sets need small tiles and the curvature correction)
+    std::vector<int> cands;
+    if (forced_variant >= 0) {
+      cands.push_back(forced_variant);
+    } else {
+      if (h->variant_table[precision][bucket] >= 0) cands.push_back(h->variant_table[precision][bucket]);
+      for (int c : split_preferences(N, M)) cands.push_back(c);
+    }
+    int shape_tt = -1, shape_cs = -1;
+    double mb[4] = {0.0, 0.0, 0.0, 0.0};
     for (size_t i = 0; i < cands.size(); ++i) {
       const Variant C = split_variant(cands[i]);
-      double bound = 0.0, curv = 0.0, lin = 0.0;
-      HOLO_TRY(tile_error_bound(p.get(), C.cs, C.tt(), &bound, &curv, &lin, s));
-      const double model_bound[3] = {bound, bound + curv, bound + curv + lin};
-      for (int m = 0; m < 3; ++m) p->model_bounds[m] = model_bound[m];
-      variant = cands[i];
-      p->err_bound = model_bound[C.model];
-      if (forced_variant < 0) {
-        // the same tiles with the cheapest pair model whose bound holds
-        for (int m = 2; m > C.model; --m) {
-          const int twin = split_twin(cands[i], m);
-          if (twin >= 0 && model_bound[m] <= kSplitBoundMetres) {
-            variant = twin;
-            p->err_bound = model_bound[m];
-            break;
-          }
-        }
+      if (C.tt() != shape_tt || C.cs != shape_cs) {
+        // tile boxes of this shape (left in tiles_s / tiles_t) and its error model
+        double bound = 0.0, curv = 0.0, lin = 0.0, gemm = 0.0;
+        HOLO_TRY(tile_error_bound(p.get(), C.cs, C.tt(), &bound, &curv, &lin, &gemm, s));
+        mb[0] = bound;
+        mb[1] = bound + curv;
+        mb[2] = mb[1] + lin;
+        mb[3] = mb[2] + gemm;
+        shape_tt = C.tt();
+        shape_cs = C.cs;
       }
+      variant = cands[i];
+      for (int m = 0; m < 4; ++m) p->model_bounds[m] = mb[m];
+      p->err_bound = mb[C.model];
       if (p->err_bound <= kSplitBoundMetres) break;
     }
   }
@@ -1033,7 +1039,7 @@ int holo_variant_describe(int precision, int variant, int *threads, int *targets
   if (source_tile) *source_tile = V.cs;
   if (fma_sincos_targets) *fma_sincos_targets = V.poly;
   if (pair_model) *pair_model = V.model;
-  if (pair_loop) *pair_loop = V.ws ? 2 : V.packed;
+  if (pair_loop) *pair_loop = V.tc ? 3 : (V.ws ? 2 : V.packed);
   return HOLO_OK;
 }
 

@@ -63,14 +63,20 @@ struct Variant {
                  //   0: c / 2r (1 + c / 4r^2) with r from rsqrt (12 FP32 + 3 MUFU)
                  //   1: c / 2r, rsqrt                             (10 FP32 + 3 MUFU)
                  //   2: c / 2q with 1/q to first order in Ps / Qt  (8 FP32 + 2 MUFU)
+                 //   3: model 2 with the phase from tcgen05 TF32 MMAs (3 FP32 + 2 MUFU)
                  // the planner takes model 1 or 2 only when its error bound allows
   int packed = 0; // 1: pair loop on packed FP32 pairs (two sources per instruction)
   int ws = 0;     // 1: warp-specialised sin/cos (`poly` is then the average per thread)
+  int tc = 0;     // 1: phase on the tensor cores (kernel_tc.cu; `poly` of 8 source pairs)
   int tt() const { return threads * r; }
 };
 
 int split_variant_count();
 Variant split_variant(int i);
+// Split variants in the planner's order of preference (fastest first) for N x M.
+std::vector<int> split_preferences(size_t N, size_t M);
+// The variant a batched (work-queue) launch runs for a plan of variant v.
+int split_batched_variant(int v);
 // The variant with the same tiles and sin/cos split as `v` and pair model
 // `model` (its packed pair loop where there is one), or -1.
 int split_twin(int v, int model);
@@ -89,9 +95,12 @@ struct TileStats {
 //   curv: the curvature term c^2 / 8r^3 that pair models 1 and 2 drop;
 //   lin:  the extra error of pair model 2 (1/q to first order in Ps / Qt, and
 //         1/q for the amplitude 1/r), its amplitude part as the phase (radians at
-//         400 nm) of the same size.
+//         400 nm) of the same size;
+//   gemm: the extra rounding of pair model 3 (3xTF32 products accumulated by the
+//         tensor core, taken as 4 FP32 ulps of the curvature term).
 // Infinite when the two point sets' boxes touch.
-void split_error_model(const TileStats &st, double *base, double *curv, double *lin);
+void split_error_model(const TileStats &st, double *base, double *curv, double *lin,
+                       double *gemm);
 // Path-length error budget of the split path: 5e-6 rad at lambda = 400 nm.
 constexpr double kSplitBoundMetres = 5e-6 * 400e-9 / (2.0 * 3.14159265358979323846);
 int fp64_variant_count();
@@ -162,6 +171,11 @@ int launch_gather_apf(const double *amp, const double *phase, const int32_t *ord
                       int n_pad, float2 *out, cudaStream_t s);
 
 // kernel_split.cu
+// kernel_tc.cu: the tensor-core split kernel (pair model 3), `npp` of 8 source pairs
+// on the FMA-pipe sin/cos
+int launch_split_tc(const SplitProblem &p, int npp, int grid, int *err, cudaStream_t s);
+int split_tc_occupancy(int npp, int *ctas_per_sm);
+int split_tc_smem_bytes();
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
                  int *err, cudaStream_t s);
 int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,
@@ -217,7 +231,7 @@ struct holo_plan_s {
   int grid = 0;
   int n_stiles = 0, n_ttiles = 0;
   double err_bound = 0.0;        // split path: bound on the path-length error (m)
-  double model_bounds[3] = {0.0, 0.0, 0.0};  // the same for pair models 0, 1, 2 (same tiles)
+  double model_bounds[4] = {0.0, 0.0, 0.0, 0.0};  // the same for pair models 0-3 (same tiles)
   cudaStream_t last_stream = nullptr;
   // device buffers
   double *pos_s = nullptr;       // 3 * n_pad

@@ -1,0 +1,416 @@
+// kernel_tc.cu -- split-precision Huygens superposition with the per-pair phase
+// on the 5th-generation tensor cores (HOLO_SPLIT32, pair model 3).
+//
+// Same frame decomposition as kernel_split.cu (cuda/superposition.cu:35-51,
+// 59-154 restated per (target tile, source tile) pair) and the same first-order
+// 1/q model as pair model 2, but the phase of every pair is one inner product
+// of per-target and per-source features in the tile-pair frame:
+//   theta'(t, s) = sign A_s + (S2 - 2 T.S) (Iq + Kq Ps) + Kq T2 Ps   (+ Iq T2 per target)
+//                = sum_k f_k(t) g_k(s) + (1, 1, 1) . (a0, a1, a2)_s,
+//   f = [Iq, -2 Iq Tx, -2 Iq Ty, Kq T2, Kq, -2 Kq Tx, -2 Kq Ty, 0],
+//   g = [S2, Sx, Sy, Ps, Ps S2, Ps Sx, Ps Sy, 0]     (Iq = |kap2| / Qt, Kq = |kap2| / Qt^2,
+//                                                    a0 + a1 + a2 = sign A in TF32 parts)
+// with Iq T2 moved into the per-target rotation.  A tile of 128 targets x 256
+// sources of theta' is one tcgen05.mma of kind::tf32 (M = 128, N = 256, K = 8)
+// per product: the geometric features in three TF32 products (hi hi + hi lo +
+// lo hi, the 3xTF32 split: ~2^-21 relative), and sign A split three ways into
+// TF32 parts against constant ones (exact products) in a second K block.  The
+// accumulator lives in tensor memory (two buffers of 256 columns); 16 consumer
+// warps read it with tcgen05.ld (warp w: TMEM lanes 32 (w % 4).., columns
+// 64 (w / 4)..), take sin/cos (MUFU, or the FMA-pipe polynomial for NPP of
+// every 8 source pairs) and accumulate a' e^{i theta'} on packed f32x2 pairs.
+// One more warp allocates the tensor memory and issues the MMAs (one thread),
+// tracked by mbarriers: full[b] (tcgen05.commit) and free[b] (16 consumer
+// arrivals).  Per pair on the CUDA cores: 3 FP32-pipe ops + 2 MUFU ops.
+//
+// Tiles: 512 targets per CTA (4 blocks of 128), 1024 sources per tile (4 blocks
+// of 256); one CTA per SM (~200 KB of shared memory).  Every wait is bounded:
+// after a timeout the kernel raises the device error word and skips the rest
+// of its work, then waits (bounded) for the MMAs it issued and frees the
+// tensor memory.
+#include "internal.cuh"
+#include "ptx.cuh"
+
+namespace holo {
+namespace {
+
+#include "split_frame.cuh"
+
+constexpr int kTcTT = 512;                    // targets per CTA
+constexpr int kTcCS = 1024;                   // sources per tile
+constexpr int kTcM = 128, kTcN = 256, kTcK = 8;
+constexpr int kTcConsumers = 16;              // consumer warps
+constexpr int kTcThreads = 32 * (kTcConsumers + 1);
+constexpr int kTcCols = 2 * kTcN;             // TMEM columns: two accumulator buffers
+constexpr uint32_t kTcLbo = 128, kTcSbo = 256;  // operand layout (bytes), see tc_off
+
+// Float offset of element (row r, feature k) of a K-major tf32 operand with K = 8:
+// core matrices of 8 rows x 4 features (16 B rows, 128 B), the two along K 128 B
+// apart (LBO), 8-row groups 256 B apart (SBO).  Rows of one 128- or 256-row block
+// are contiguous, so block b starts at row 128 b / 256 b.
+__host__ __device__ __forceinline__ int tc_off(int r, int k) {
+  return (r >> 3) * 64 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3);
+}
+
+struct TcSmem {
+  static constexpr size_t raw_geo = 0;                                 // float [CS*6]
+  static constexpr size_t raw_apf = raw_geo + kTcCS * 6 * 4;           // float2 [CS]
+  static constexpr size_t opb_hi = raw_apf + kTcCS * 8;                // float [CS*8]
+  static constexpr size_t opb_lo = opb_hi + kTcCS * kTcK * 4;          // float [CS*8]
+  static constexpr size_t opb_a = opb_lo + kTcCS * kTcK * 4;           // float [CS*8]: A parts
+  static constexpr size_t opa_hi = opb_a + kTcCS * kTcK * 4;           // float [TT*8]
+  static constexpr size_t opa_lo = opa_hi + kTcTT * kTcK * 4;          // float [TT*8]
+  static constexpr size_t opa_one = opa_lo + kTcTT * kTcK * 4;         // float [128*8]: (1,1,1,0..)
+  static constexpr size_t amp = opa_one + kTcM * kTcK * 4;             // float [CS]
+  static constexpr size_t part = amp + kTcCS * 4;                      // float2 [4][TT]
+  static constexpr size_t acc = part + 4 * kTcTT * 8;                  // double2 [TT]
+  static constexpr size_t tph = acc + kTcTT * 16;                      // float [TT]
+  static constexpr size_t tsc = tph + kTcTT * 4;                       // float [TT]
+  static constexpr size_t frame = tsc + kTcTT * 4;                     // Frame
+  static constexpr size_t bars = (frame + sizeof(Frame) + 15) / 16 * 16;  // uint64 [5]
+  static constexpr size_t misc = bars + 5 * 8;                         // uint32 taddr, abort
+  static constexpr size_t bytes = misc + 16;
+};
+static_assert(TcSmem::bytes <= 227 * 1024, "tensor-core split kernel: shared memory");
+static_assert(TcSmem::opb_hi % 128 == 0 && TcSmem::opa_hi % 128 == 0 && TcSmem::opa_one % 16 == 0,
+              "operand alignment");
+
+__device__ __forceinline__ void split_range_tc(int n, int splits, int s, int *b, int *e) {
+  *b = (int)(((long long)n * s) / splits);
+  *e = (int)(((long long)n * (s + 1)) / splits);
+}
+
+// Bounded wait that gives up at once when the CTA has aborted.
+__device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                                        int *err) {
+  if (*abort_flag) return false;
+  if (ptx::mbar_wait_bounded(bar, parity, kWaitCycles)) return true;
+  *abort_flag = 1;
+  atomicExch(err, kDevErrTimeout);
+  return false;
+}
+
+template <int NPP>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_split_tc(const SplitProblem P, int n_items, int *err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  using L = TcSmem;
+  float *raw_geo = reinterpret_cast<float *>(smem + L::raw_geo);
+  float2 *raw_apf = reinterpret_cast<float2 *>(smem + L::raw_apf);
+  float *opb_hi = reinterpret_cast<float *>(smem + L::opb_hi);
+  float *opb_lo = reinterpret_cast<float *>(smem + L::opb_lo);
+  float *opb_a = reinterpret_cast<float *>(smem + L::opb_a);
+  float *opa_hi = reinterpret_cast<float *>(smem + L::opa_hi);
+  float *opa_lo = reinterpret_cast<float *>(smem + L::opa_lo);
+  float *opa_one = reinterpret_cast<float *>(smem + L::opa_one);
+  float *amp = reinterpret_cast<float *>(smem + L::amp);
+  float2 *part = reinterpret_cast<float2 *>(smem + L::part);
+  double2 *acc = reinterpret_cast<double2 *>(smem + L::acc);
+  float *tph = reinterpret_cast<float *>(smem + L::tph);
+  float *tsc = reinterpret_cast<float *>(smem + L::tsc);
+  Frame *fr = reinterpret_cast<Frame *>(smem + L::frame);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bars);
+  uint64_t *bar_tma = bars, *full = bars + 1, *freeb = bars + 3;
+  uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(smem + L::misc);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + L::misc + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool producer = warp == kTcConsumers;
+  constexpr int NC = kTcConsumers * 32;  // consumer threads
+
+  if (tid == 0) {
+    ptx::mbar_init(bar_tma, 1);
+    ptx::mbar_init(&full[0], 1);
+    ptx::mbar_init(&full[1], 1);
+    ptx::mbar_init(&freeb[0], kTcConsumers);
+    ptx::mbar_init(&freeb[1], kTcConsumers);
+    *abort_flag = 0;
+    ptx::fence_barrier_init();
+  }
+  // constant operand of the phase term: every row (1, 1, 1, 0, ..)
+  for (int i = tid; i < kTcM * kTcK; i += kTcThreads)
+    opa_one[tc_off(i / kTcK, i % kTcK)] = (i % kTcK) < 3 ? 1.f : 0.f;
+  if (producer) ptx::tmem_alloc(taddr_slot, kTcCols);
+  ptx::fence_proxy_async_smem();
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tbase = *taddr_slot;
+
+  const double sk = P.sk;
+  const float kap2 = (float)(0.5 * sk), ak = fabsf(kap2), iak = 1.f / fabsf(kap2);
+  const float sgn = kap2 < 0.f ? -1.f : 1.f;
+  constexpr uint32_t idesc = ptx::tc_idesc_tf32(kTcM, kTcN);
+  uint32_t par_tma = 0;
+  // producer: MMA groups issued per TMEM buffer; consumers: completions consumed
+  uint32_t uses[2] = {0u, 0u};
+
+  auto issue = [&](int j) {
+    ptx::mbar_arrive_expect_tx(bar_tma, kTcCS * (6 * sizeof(float) + sizeof(float2)));
+    ptx::bulk_g2s(raw_geo, P.geo_s + (size_t)j * kTcCS * 6, kTcCS * 6 * sizeof(float), bar_tma);
+    ptx::bulk_g2s(raw_apf, P.apf_s + (size_t)j * kTcCS, kTcCS * sizeof(float2), bar_tma);
+  };
+
+  for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const int tt = item / P.splits, split = item % P.splits;
+    int sb, se;
+    split_range_tc(P.n_stiles, P.splits, split, &sb, &se);
+    for (int t = tid; t < kTcTT; t += kTcThreads) acc[t] = make_double2(0.0, 0.0);
+    if (tid == 0 && sb < se && !*abort_flag) issue(sb);
+
+    for (int j = sb; j < se; ++j) {
+      if (tid == 0)
+        build_frame(fr, P.tiles_t + 6 * (size_t)tt, P.tiles_s + 6 * (size_t)j, sk);
+      tc_wait(bar_tma, par_tma, abort_flag, err);
+      par_tma ^= 1u;
+      __syncthreads();  // frame and staged records visible
+
+      // ---- operands of this tile pair (consumer threads) ----
+      if (!producer && !*abort_flag) {
+        const float f1x = fr->e1[0], f1y = fr->e1[1], f1z = fr->e1[2];
+        const float f2x = fr->e2[0], f2y = fr->e2[1], f2z = fr->e2[2];
+        const float fex = fr->ef[0], fey = fr->ef[1], fez = fr->ef[2];
+        const float ir0 = fr->r0f > 0.f ? 1.f / fr->r0f : 0.f;
+        float ah[3], al[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          ah[d] = fr->ah[d];
+          al[d] = fr->al[d];
+        }
+        for (int i = tid; i < kTcCS; i += NC) {
+          float g[kTcK] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+          float a3[3] = {0.f, 0.f, 0.f}, am = 0.f;
+          if (j * kTcCS + i < P.N) {
+            const float *q = raw_geo + 6 * i;
+            const float sh[3] = {q[0], q[1], q[2]}, sl[3] = {q[3], q[4], q[5]};
+            const float2 pa = raw_apf[i];
+            float S, E, S2, E2;
+            dot3_ff(ah, al, sh, sl, S, E);
+            two_sum(pa.x, -S, S2, E2);
+            const float sA = sgn * reduce_two_pi_ff(S2, __fsub_rn(E2, E));
+            const float Sx = fmaf(f1x, sh[0], fmaf(f1y, sh[1], f1z * sh[2]));
+            const float Sy = fmaf(f2x, sh[0], fmaf(f2y, sh[1], f2z * sh[2]));
+            const float Ps = fmaf(fex, sh[0], fmaf(fey, sh[1], fez * sh[2]));
+            const float s2 = fmaf(Sx, Sx, Sy * Sy);
+            g[0] = s2; g[1] = Sx; g[2] = Sy; g[3] = Ps;
+            g[4] = Ps * s2; g[5] = Ps * Sx; g[6] = Ps * Sy;
+            // sign A = a0 + a1 + a2 exactly, each part a TF32 number
+            a3[0] = ptx::to_tf32(sA);
+            const float r1 = __fsub_rn(sA, a3[0]);
+            a3[1] = ptx::to_tf32(r1);
+            a3[2] = ptx::to_tf32(__fsub_rn(r1, a3[1]));
+            am = pa.y * fmaf(Ps, ir0, 1.f);
+          }
+#pragma unroll
+          for (int k = 0; k < kTcK; ++k) {
+            const float hi = ptx::to_tf32(g[k]);
+            opb_hi[tc_off(i, k)] = hi;
+            opb_lo[tc_off(i, k)] = ptx::to_tf32(__fsub_rn(g[k], hi));
+            opb_a[tc_off(i, k)] = k < 3 ? a3[k] : 0.f;
+          }
+          amp[i] = am;
+        }
+        // targets: one per consumer thread
+        {
+          const int t = tid;
+          const int ti = tt * kTcTT + t;
+          float th[3] = {0.f, 0.f, 0.f}, tl[3] = {0.f, 0.f, 0.f};
+          if (ti < P.M) {
+            const float *q = P.geo_t + 6 * (size_t)ti;
+            th[0] = q[0]; th[1] = q[1]; th[2] = q[2];
+            tl[0] = q[3]; tl[1] = q[4]; tl[2] = q[5];
+          }
+          float S, E, S2, E2;
+          dot3_ff(ah, al, th, tl, S, E);
+          two_sum(S, fr->b0h, S2, E2);
+          const float B = reduce_two_pi_ff(S2, __fadd_rn(__fadd_rn(E, E2), fr->b0l));
+          const float Tx = fmaf(f1x, th[0], fmaf(f1y, th[1], f1z * th[2]));
+          const float Ty = fmaf(f2x, th[0], fmaf(f2y, th[1], f2z * th[2]));
+          const float Qt = fr->r0f + fmaf(fex, th[0], fmaf(fey, th[1], fez * th[2]));
+          const float T2 = fmaf(Tx, Tx, Ty * Ty);
+          const float Iq = ak / Qt, Kq = Iq / Qt;
+          const float f[kTcK] = {Iq, -2.f * Iq * Tx, -2.f * Iq * Ty, Kq * T2,
+                                 Kq, -2.f * Kq * Tx, -2.f * Kq * Ty, 0.f};
+#pragma unroll
+          for (int k = 0; k < kTcK; ++k) {
+            const float hi = ptx::to_tf32(f[k]);
+            opa_hi[tc_off(t, k)] = hi;
+            opa_lo[tc_off(t, k)] = ptx::to_tf32(__fsub_rn(f[k], hi));
+          }
+          tph[t] = B + sgn * Iq * T2;  // the target's rotation, incl. the Iq T2 term
+          tsc[t] = Iq * iak;           // 1 / Qt
+        }
+      }
+      ptx::fence_proxy_async_smem();
+      ptx::tc_fence_before();
+      __syncthreads();  // operands complete; the staging buffer is free
+      ptx::tc_fence_after();
+      if (tid == 0 && j + 1 < se && !*abort_flag) issue(j + 1);
+
+      if (producer) {
+        // ---- MMA issue: 4 target blocks x 4 source blocks, double-buffered ----
+        if (lane == 0) {
+          for (int blk = 0; blk < 16; ++blk) {
+            const int m = blk >> 2, n = blk & 3, b = blk & 1;
+            if (uses[b] > 0) tc_wait(&freeb[b], (uses[b] - 1) & 1u, abort_flag, err);
+            if (*abort_flag) break;
+            ptx::tc_fence_after();
+            const uint32_t d = tbase + (uint32_t)(b * kTcN);
+            const uint64_t dah = ptx::tc_smem_desc(opa_hi + m * kTcM * kTcK, kTcLbo, kTcSbo);
+            const uint64_t dal = ptx::tc_smem_desc(opa_lo + m * kTcM * kTcK, kTcLbo, kTcSbo);
+            const uint64_t dbh = ptx::tc_smem_desc(opb_hi + n * kTcN * kTcK, kTcLbo, kTcSbo);
+            const uint64_t dbl = ptx::tc_smem_desc(opb_lo + n * kTcN * kTcK, kTcLbo, kTcSbo);
+            const uint64_t dba = ptx::tc_smem_desc(opb_a + n * kTcN * kTcK, kTcLbo, kTcSbo);
+            const uint64_t d1 = ptx::tc_smem_desc(opa_one, kTcLbo, kTcSbo);
+            ptx::tc_mma_tf32(d, dah, dbh, idesc, 0u);
+            ptx::tc_mma_tf32(d, dah, dbl, idesc, 1u);
+            ptx::tc_mma_tf32(d, dal, dbh, idesc, 1u);
+            ptx::tc_mma_tf32(d, d1, dba, idesc, 1u);
+            ptx::tc_commit(&full[b]);
+            ++uses[b];
+          }
+        }
+        __syncwarp();
+      } else {
+        // ---- consumers: sin/cos and accumulation of a' e^{i theta'} ----
+        const int lg = warp & 3, cg = warp >> 2;
+        for (int m = 0; m < 4; ++m) {
+          uint64_t re2 = 0ull, im2 = 0ull;
+          for (int n = 0; n < 4; ++n) {
+            const int b = (m * 4 + n) & 1;
+            const bool ok =
+                __all_sync(0xffffffffu, tc_wait(&full[b], uses[b] & 1u, abort_flag, err));
+            ++uses[b];
+            ptx::tc_fence_after();
+            if (ok) {
+#pragma unroll 1
+              for (int ch = 0; ch < 4; ++ch) {
+                const int col = cg * 64 + ch * 16;
+                float th[16];
+                ptx::tmem_ld16(tbase + ((uint32_t)(32 * lg) << 16) + (uint32_t)(b * kTcN + col),
+                               th);
+                const float4 *ap = reinterpret_cast<const float4 *>(amp + n * kTcN + col);
+                float av[16];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                  const float4 v = ap[q];
+                  av[4 * q] = v.x;
+                  av[4 * q + 1] = v.y;
+                  av[4 * q + 2] = v.z;
+                  av[4 * q + 3] = v.w;
+                }
+#pragma unroll
+                for (int pp = 0; pp < 8; ++pp) {
+                  const uint64_t t2 = ptx::pack2(th[2 * pp], th[2 * pp + 1]);
+                  const uint64_t am = ptx::pack2(av[2 * pp], av[2 * pp + 1]);
+                  uint64_t sn, cs;
+                  if (pp < NPP) {
+                    poly_sincos2(t2, sn, cs);  // FMA pipe
+                  } else {
+                    const float t0 = th[2 * pp], t1 = th[2 * pp + 1];
+                    sn = ptx::pack2(ptx::sin_approx(t0), ptx::sin_approx(t1));  // XU pipe
+                    cs = ptx::pack2(ptx::cos_approx(t0), ptx::cos_approx(t1));
+                  }
+                  re2 = ptx::fma2(am, cs, re2);
+                  im2 = ptx::fma2(am, sn, im2);
+                }
+              }
+            }
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&freeb[b]);
+          }
+          float x, y;
+          ptx::unpack2(re2, x, y);
+          const float re = x + y;
+          ptx::unpack2(im2, x, y);
+          part[cg * kTcTT + m * kTcM + 32 * lg + lane] = make_float2(re, x + y);
+        }
+      }
+      __syncthreads();  // partial sums complete
+
+      // ---- per target: sum the four column groups, scale, rotate, carry in FP64 ----
+      if (!producer) {
+        const int t = tid;
+        const float2 s0 = part[t], s1 = part[kTcTT + t], s2 = part[2 * kTcTT + t],
+                     s3 = part[3 * kTcTT + t];
+        const float sc = tsc[t];
+        const float re = ((s0.x + s1.x) + (s2.x + s3.x)) * sc;
+        const float im = sgn * ((s0.y + s1.y) + (s2.y + s3.y)) * sc;
+        float sr, cr;
+        __sincosf(tph[t], &sr, &cr);
+        double2 a = acc[t];
+        a.x += (double)fmaf(re, cr, -im * sr);
+        a.y += (double)fmaf(re, sr, im * cr);
+        acc[t] = a;
+      }
+      __syncthreads();  // operands, partials and per-target data are rewritten next tile
+    }
+
+    for (int t = tid; t < kTcTT; t += kTcThreads) {
+      const int ti = tt * kTcTT + t;
+      if (ti < P.M) {
+        const double2 v = acc[t];
+        if (P.splits == 1)
+          P.y[P.order_t[ti]] = v;
+        else
+          P.partial[(size_t)split * P.M + ti] = v;
+      }
+    }
+    __syncthreads();  // acc is reset by the next item
+  }
+
+  // ---- teardown: the MMAs this CTA issued have completed, then free the TMEM ----
+  if (producer && lane == 0)
+    for (int b = 0; b < 2; ++b)
+      if (uses[b] > 0) ptx::mbar_wait_bounded(&full[b], (uses[b] - 1) & 1u, kWaitCycles);
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  if (producer) ptx::tmem_dealloc(tbase, kTcCols);
+}
+
+template <int NPP>
+int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
+  auto kern = k_split_tc<NPP>;
+  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)TcSmem::bytes));
+  const int n_items = p.n_ttiles * p.splits;
+  if (n_items <= 0) return HOLO_OK;
+  kern<<<grid, kTcThreads, TcSmem::bytes, s>>>(p, n_items, err);
+  note_launches(1);
+  HOLO_CUDA(cudaGetLastError());
+  return HOLO_OK;
+}
+
+template <int NPP>
+int occupancy_tc(int *out) {
+  auto kern = k_split_tc<NPP>;
+  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)TcSmem::bytes));
+  HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, kTcThreads, TcSmem::bytes));
+  return HOLO_OK;
+}
+
+}  // namespace
+
+int launch_split_tc(const SplitProblem &p, int npp, int grid, int *err, cudaStream_t s) {
+  switch (npp) {
+    case 2: return launch_tc<2>(p, grid, err, s);
+    case 3: return launch_tc<3>(p, grid, err, s);
+    case 4: return launch_tc<4>(p, grid, err, s);
+    default: return fail(HOLO_ERR_INVALID, "tensor-core split kernel: no build for %d of 8", npp);
+  }
+}
+
+int split_tc_occupancy(int npp, int *ctas_per_sm) {
+  switch (npp) {
+    case 2: return occupancy_tc<2>(ctas_per_sm);
+    case 3: return occupancy_tc<3>(ctas_per_sm);
+    case 4: return occupancy_tc<4>(ctas_per_sm);
+    default: return fail(HOLO_ERR_INVALID, "tensor-core split kernel: no build for %d of 8", npp);
+  }
+}
+
+int split_tc_smem_bytes() { return (int)TcSmem::bytes; }
+
+}  // namespace holo

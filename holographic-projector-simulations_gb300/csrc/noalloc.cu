@@ -104,7 +104,8 @@ struct Carve {
 };
 
 // The error model of the allocating planner, from the 20 tile statistics.
-void model_from_stats(const double *st, double *base, double *curv, double *lin) {
+void model_from_stats(const double *st, double *base, double *curv, double *lin,
+                      double *gemm) {
   TileStats t;
   for (int d = 0; d < 3; ++d) {
     t.lo_s[d] = st[d];
@@ -116,7 +117,7 @@ void model_from_stats(const double *st, double *base, double *curv, double *lin)
   }
   t.h_s = st[6];
   t.h_t = st[16];
-  split_error_model(t, base, curv, lin);
+  split_error_model(t, base, curv, lin, gemm);
 }
 
 bool is_device_pointer(const void *p) {
@@ -190,36 +191,34 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
   HOLO_TRY(sort_points(v, (int)M, bbox, order_t, keys, hist, scan, s));
   HOLO_TRY(launch_gather_pos(v, order_t, (int)M, (int)M, pos_t, s));
 
-  // ---- tile size: the largest whose path-length error bound holds ----
-  const int cands[] = {9, 11, 3, 4};
+  // ---- kernel: the planner's preference list, first whose error bound holds ----
+  const std::vector<int> cands = split_preferences(N, M);
   const double budget = kSplitBoundMetres;
   int variant = cands[0];
-  for (int i = 0; i < 4; ++i) {
-    if (M < 1024 && (cands[i] == 9 || cands[i] == 11)) continue;
+  int shape_tt = -1, shape_cs = -1;
+  double mb[4] = {0.0, 0.0, 0.0, 0.0};
+  for (size_t i = 0; i < cands.size(); ++i) {
     const Variant C = split_variant(cands[i]);
-    const int ns = (int)((N + C.cs - 1) / C.cs), nt = (int)((M + C.tt() - 1) / C.tt());
-    HOLO_TRY(launch_tile_bbox(pos_s, (int)N, C.cs, tiles_s, s));
-    HOLO_TRY(launch_tile_bbox(pos_t, (int)M, C.tt(), tiles_t, s));
-    k_tile_stats<<<1, 256, 0, s>>>(tiles_s, ns, tiles_t, nt, stats);
-    HOLO_CUDA(cudaGetLastError());
-    double st[20];
-    HOLO_CUDA(cudaMemcpyAsync(st, stats, sizeof(st), cudaMemcpyDeviceToHost, s));
-    HOLO_CUDA(cudaStreamSynchronize(s));
-    double base = 0.0, curv = 0.0, lin = 0.0;
-    model_from_stats(st, &base, &curv, &lin);
-    const double model_bound[3] = {base, base + curv, base + curv + lin};
-    variant = cands[i];
-    bool ok = model_bound[0] <= budget;
-    // the same tiles with the cheapest pair model whose bound holds
-    for (int m = 2; m > 0; --m) {
-      const int twin = split_twin(cands[i], m);
-      if (twin >= 0 && model_bound[m] <= budget) {
-        variant = twin;
-        ok = true;
-        break;
-      }
+    if (C.tt() != shape_tt || C.cs != shape_cs) {
+      const int ns = (int)((N + C.cs - 1) / C.cs), nt = (int)((M + C.tt() - 1) / C.tt());
+      HOLO_TRY(launch_tile_bbox(pos_s, (int)N, C.cs, tiles_s, s));
+      HOLO_TRY(launch_tile_bbox(pos_t, (int)M, C.tt(), tiles_t, s));
+      k_tile_stats<<<1, 256, 0, s>>>(tiles_s, ns, tiles_t, nt, stats);
+      HOLO_CUDA(cudaGetLastError());
+      double st[20];
+      HOLO_CUDA(cudaMemcpyAsync(st, stats, sizeof(st), cudaMemcpyDeviceToHost, s));
+      HOLO_CUDA(cudaStreamSynchronize(s));
+      double base = 0.0, curv = 0.0, lin = 0.0, gemm = 0.0;
+      model_from_stats(st, &base, &curv, &lin, &gemm);
+      mb[0] = base;
+      mb[1] = base + curv;
+      mb[2] = mb[1] + lin;
+      mb[3] = mb[2] + gemm;
+      shape_tt = C.tt();
+      shape_cs = C.cs;
     }
-    if (ok) break;
+    variant = cands[i];
+    if (mb[C.model] <= budget) break;
   }
   const Variant V = split_variant(variant);
   // the last bound evaluation left this variant's tile boxes in tiles_s / tiles_t
