@@ -222,6 +222,13 @@ def run_profile_case(args):
     dev = torch.device("cuda", 0)
     t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
     args_ = (t(amp), t(phase), t(u), t(vv))
+    if args.variants:  # one forced kernel variant instead of the planner's choice
+        var = int(args.variants.split(",")[0])
+        for _ in range(2):
+            holo.transform(*args_, -1, LAM, precision=args.precision, variant=var)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": {"variant": var}, "pairs_per_launch": len(amp) * len(vv)}))
+        return
     with holo.Plan(args_[2], args_[3], args.precision) as pl:
         for _ in range(2):
             pl.execute(args_[0], args_[1], -1, LAM)
@@ -395,7 +402,8 @@ def main():
                     help="small case for ncu: two split-FP32 passes of the 512^2 sources onto "
                          "a 256^2 patch of the projector (1.7e10 pairs each), then exit")
     ap.add_argument("--variants", default="",
-                    help="comma-separated variant numbers to restrict --sweep-variants to")
+                    help="comma-separated variant numbers to restrict --sweep-variants to "
+                         "(--profile-case: the first one is forced)")
     ap.add_argument("--sweep-variants", action="store_true",
                     help="time every split-FP32 kernel variant on the config-2 y pass, then exit")
     ap.add_argument("--workload", default="config2",

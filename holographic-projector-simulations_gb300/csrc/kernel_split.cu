@@ -567,8 +567,9 @@ int split_batched_variant(int v) { return is_tc(v) ? kTcFallback : v; }
 std::vector<int> split_preferences(size_t N, size_t M) {
   (void)N;
   if (M < 1024) return {3, 4};
-  // fastest first: the CUDA-core pair models 2, 1, 0 on ever smaller tiles
-  return {23, 13, 9, 27, 21, 16, 11, 3, 4};
+  // fastest first: the tensor-core phase (pair model 3), then the CUDA-core pair
+  // models 2, 1, 0 on ever smaller tiles
+  return {34, 23, 13, 9, 27, 21, 16, 11, 3, 4};
 }
 
 int split_twin(int v, int model) {

@@ -66,8 +66,8 @@ struct TcSmem {
   static constexpr size_t acc = part + 4 * kTcTT * 8;                  // double2 [TT]
   static constexpr size_t tph = acc + kTcTT * 16;                      // float [TT]
   static constexpr size_t tsc = tph + kTcTT * 4;                       // float [TT]
-  static constexpr size_t frame = tsc + kTcTT * 4;                     // Frame
-  static constexpr size_t bars = (frame + sizeof(Frame) + 15) / 16 * 16;  // uint64 [5]
+  static constexpr size_t frame = tsc + kTcTT * 4;                     // Frame [2]
+  static constexpr size_t bars = (frame + 2 * sizeof(Frame) + 15) / 16 * 16;  // uint64 [5]
   static constexpr size_t misc = bars + 5 * 8;                         // uint32 taddr, abort
   static constexpr size_t bytes = misc + 16;
 };
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   double2 *acc = reinterpret_cast<double2 *>(smem + L::acc);
   float *tph = reinterpret_cast<float *>(smem + L::tph);
   float *tsc = reinterpret_cast<float *>(smem + L::tsc);
-  Frame *fr = reinterpret_cast<Frame *>(smem + L::frame);
+  Frame *frames = reinterpret_cast<Frame *>(smem + L::frame);  // tile j in frames[j & 1]
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bars);
   uint64_t *bar_tma = bars, *full = bars + 1, *freeb = bars + 3;
   uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(smem + L::misc);
@@ -158,7 +158,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (tid == 0 && sb < se && !*abort_flag) issue(sb);
 
     for (int j = sb; j < se; ++j) {
-      if (tid == 0)
+      Frame *fr = frames + (j & 1);
+      // the first tile's frame here; the next ones by the MMA warp during the
+      // previous tile's pair work
+      if (tid == 0 && j == sb)
         build_frame(fr, P.tiles_t + 6 * (size_t)tt, P.tiles_s + 6 * (size_t)j, sk);
       tc_wait(bar_tma, par_tma, abort_flag, err);
       par_tma ^= 1u;
@@ -248,6 +251,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
       if (producer) {
         // ---- MMA issue: 4 target blocks x 4 source blocks, double-buffered ----
+        if (lane == 1 && j + 1 < se)
+          build_frame(frames + ((j + 1) & 1), P.tiles_t + 6 * (size_t)tt,
+                      P.tiles_s + 6 * (size_t)(j + 1), sk);
         if (lane == 0) {
           for (int blk = 0; blk < 16; ++blk) {
             const int m = blk >> 2, n = blk & 3, b = blk & 1;
@@ -282,13 +288,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             ++uses[b];
             ptx::tc_fence_after();
             if (ok) {
-#pragma unroll 1
+              // the load of chunk ch + 1 is in flight while chunk ch is summed
+              const uint32_t ta =
+                  tbase + ((uint32_t)(32 * lg) << 16) + (uint32_t)(b * kTcN + cg * 64);
+              uint32_t rv[2][16];
+              ptx::tmem_ld16_nowait(ta, rv[0]);
+              ptx::tmem_wait16(rv[0]);
+#pragma unroll
               for (int ch = 0; ch < 4; ++ch) {
-                const int col = cg * 64 + ch * 16;
-                float th[16];
-                ptx::tmem_ld16(tbase + ((uint32_t)(32 * lg) << 16) + (uint32_t)(b * kTcN + col),
-                               th);
-                const float4 *ap = reinterpret_cast<const float4 *>(amp + n * kTcN + col);
+                if (ch < 3) ptx::tmem_ld16_nowait(ta + (uint32_t)(16 * (ch + 1)), rv[(ch + 1) & 1]);
+                const float4 *ap =
+                    reinterpret_cast<const float4 *>(amp + n * kTcN + cg * 64 + 16 * ch);
                 float av[16];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -298,21 +308,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                   av[4 * q + 2] = v.z;
                   av[4 * q + 3] = v.w;
                 }
+                const uint32_t *th = rv[ch & 1];
 #pragma unroll
                 for (int pp = 0; pp < 8; ++pp) {
-                  const uint64_t t2 = ptx::pack2(th[2 * pp], th[2 * pp + 1]);
+                  const float t0 = __uint_as_float(th[2 * pp]);
+                  const float t1 = __uint_as_float(th[2 * pp + 1]);
+                  const uint64_t t2 = ptx::pack2(t0, t1);
                   const uint64_t am = ptx::pack2(av[2 * pp], av[2 * pp + 1]);
                   uint64_t sn, cs;
                   if (pp < NPP) {
                     poly_sincos2(t2, sn, cs);  // FMA pipe
                   } else {
-                    const float t0 = th[2 * pp], t1 = th[2 * pp + 1];
                     sn = ptx::pack2(ptx::sin_approx(t0), ptx::sin_approx(t1));  // XU pipe
                     cs = ptx::pack2(ptx::cos_approx(t0), ptx::cos_approx(t1));
                   }
                   re2 = ptx::fma2(am, cs, re2);
                   im2 = ptx::fma2(am, sn, im2);
                 }
+                if (ch < 3) ptx::tmem_wait16(rv[(ch + 1) & 1]);
               }
             }
             ptx::tc_fence_before();
