@@ -117,14 +117,6 @@ struct Scratch {
   }
 };
 
-int default_split_variant(size_t N, size_t M) {
-  (void)N;
-  // measured on GB300 (config-2 y pass): 256 x 4 targets, 1024-source tiles,
-  // 1 of 4 targets per thread on the FMA-pipe sin/cos is fastest
-  if (M >= 1024) return 9;
-  return 3;
-}
-
 int default_fp64_variant(size_t N, size_t M) {
   (void)N;
   (void)M;
@@ -313,10 +305,12 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
   const int bucket = size_bucket(N, M);
   const int nv = precision == HOLO_SPLIT32 ? split_variant_count() : fp64_variant_count();
   if (forced_variant >= nv) return fail(HOLO_ERR_INVALID, "variant %d out of range", forced_variant);
+  // FP64: the forced, tuned or default variant; split: chosen below by error bound
   int variant = forced_variant;
-  if (variant < 0) variant = h->variant_table[precision][bucket];
-  if (variant < 0)
-    variant = precision == HOLO_SPLIT32 ? default_split_variant(N, M) : default_fp64_variant(N, M);
+  if (variant < 0 && precision == HOLO_FP64) {
+    variant = h->variant_table[precision][bucket];
+    if (variant < 0) variant = default_fp64_variant(N, M);
+  }
 
   if (precision == HOLO_SPLIT32) {
     // sort once; pad sources to a multiple of every source tile size

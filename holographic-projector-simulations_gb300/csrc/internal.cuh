@@ -64,7 +64,7 @@ struct Variant {
                  //   1: c / 2r, rsqrt                             (10 FP32 + 3 MUFU)
                  //   2: c / 2q with 1/q to first order in Ps / Qt  (8 FP32 + 2 MUFU)
                  //   3: model 2 with the phase from tcgen05 TF32 MMAs (3 FP32 + 2 MUFU)
-                 // the planner takes model 1 or 2 only when its error bound allows
+                 // the planner takes models 1-3 only where their error bound holds
   int packed = 0; // 1: pair loop on packed FP32 pairs (two sources per instruction)
   int ws = 0;     // 1: warp-specialised sin/cos (`poly` is then the average per thread)
   int tc = 0;     // 1: phase on the tensor cores (kernel_tc.cu; `poly` of 8 source pairs)
@@ -77,9 +77,6 @@ Variant split_variant(int i);
 std::vector<int> split_preferences(size_t N, size_t M);
 // The variant a batched (work-queue) launch runs for a plan of variant v.
 int split_batched_variant(int v);
-// The variant with the same tiles and sin/cos split as `v` and pair model
-// `model` (its packed pair loop where there is one), or -1.
-int split_twin(int v, int model);
 
 // Largest tile boxes of a source and a target tiling: per set the bounding box
 // of all tiles (lo, hi), the largest tile half-diagonal h and the largest
@@ -175,13 +172,11 @@ int launch_gather_apf(const double *amp, const double *phase, const int32_t *ord
 // on the FMA-pipe sin/cos
 int launch_split_tc(const SplitProblem &p, int npp, int grid, int *err, cudaStream_t s);
 int split_tc_occupancy(int npp, int *ctas_per_sm);
-int split_tc_smem_bytes();
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
                  int *err, cudaStream_t s);
 int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,
                          int *queue, int variant, int grid, int *err, cudaStream_t s);
 int split_occupancy(int variant, bool mc, int *ctas_per_sm);
-int split_smem_bytes(int variant);
 
 // kernel_fp64.cu
 int launch_fp64(const Fp64Problem &p, int variant, int grid, bool const_phase, int *err,

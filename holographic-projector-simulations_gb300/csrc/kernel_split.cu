@@ -572,19 +572,6 @@ std::vector<int> split_preferences(size_t N, size_t M) {
   return {34, 23, 13, 9, 27, 21, 16, 11, 3, 4};
 }
 
-int split_twin(int v, int model) {
-  if (v < 0 || v >= kNumVariants) return -1;
-  const Variant &A = kVariants[v];
-  int best = -1;
-  for (int i = 0; i < kNumVariants; ++i) {
-    const Variant &B = kVariants[i];
-    if (B.model == model && B.threads == A.threads && B.r == A.r && B.cs == A.cs &&
-        B.poly == A.poly && B.ws == A.ws && (best < 0 || B.packed > kVariants[best].packed))
-      best = i;  // the packed pair loop where there is one
-  }
-  return best;
-}
-
 #define HOLO_SPLIT_DISPATCH(V, CALL)                      \
   switch (V) {                                            \
     case 0: return CALL(256, 8, 1024, 0);                 \
@@ -648,13 +635,6 @@ int split_occupancy(int variant, bool mc, int *ctas_per_sm) {
     variant = kTcFallback;
   }
 #define CALL(T, R, C, P) occupancy_variant<T, R, C, P>(mc, ctas_per_sm)
-  HOLO_SPLIT_DISPATCH(variant, CALL)
-#undef CALL
-}
-
-int split_smem_bytes(int variant) {
-  if (is_tc(variant)) return split_tc_smem_bytes();
-#define CALL(T, R, C, P) (int)SplitSmem<T, R, C>::bytes
   HOLO_SPLIT_DISPATCH(variant, CALL)
 #undef CALL
 }

@@ -424,6 +424,4 @@ int split_tc_occupancy(int npp, int *ctas_per_sm) {
   }
 }
 
-int split_tc_smem_bytes() { return (int)TcSmem::bytes; }
-
 }  // namespace holo
