@@ -46,8 +46,8 @@ def pipe_ops_per_pair(variant: dict) -> tuple[float, float]:
     f = variant["fma_sincos_targets"] / variant["targets_per_thread"]
     if variant.get("pair_loop", 0) == 2:
         f = 0.25
-    if variant.get("pair_loop", 0) == 3:  # tensor-core phase: `fma_sincos_targets` of 8 pairs
-        f = variant["fma_sincos_targets"] / 8.0
+    if variant.get("pair_loop", 0) == 3:  # tensor-core phase: `fma_sincos_targets` of 16 pairs
+        f = variant["fma_sincos_targets"] / 16.0
     mufu, fp32 = {0: (3.0, 12.0), 1: (3.0, 10.0), 2: (2.0, 8.0),
                   3: (2.0, 3.0)}[variant.get("pair_model", 0)]
     return mufu - 2.0 * f, fp32 + 16.0 * f

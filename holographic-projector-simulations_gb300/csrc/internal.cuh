@@ -67,7 +67,8 @@ struct Variant {
                  // the planner takes models 1-3 only where their error bound holds
   int packed = 0; // 1: pair loop on packed FP32 pairs (two sources per instruction)
   int ws = 0;     // 1: warp-specialised sin/cos (`poly` is then the average per thread)
-  int tc = 0;     // 1: phase on the tensor cores (kernel_tc.cu; `poly` of 8 source pairs)
+  int tc = 0;     // 1: phase on the tensor cores (kernel_tc.cu; `poly` of 16 source pairs)
+  int sc = 0;     // tc only: MUFU pairs accumulated in scalar FP32
   int tt() const { return threads * r; }
 };
 
@@ -168,10 +169,11 @@ int launch_gather_apf(const double *amp, const double *phase, const int32_t *ord
                       int n_pad, float2 *out, cudaStream_t s);
 
 // kernel_split.cu
-// kernel_tc.cu: the tensor-core split kernel (pair model 3), `npp` of 8 source pairs
-// on the FMA-pipe sin/cos
-int launch_split_tc(const SplitProblem &p, int npp, int grid, int *err, cudaStream_t s);
-int split_tc_occupancy(int npp, int *ctas_per_sm);
+// kernel_tc.cu: the tensor-core split kernel (pair model 3), `poly16` of every 16
+// source pairs on the FMA-pipe sin/cos, `scalar`: MUFU pairs accumulated unpacked
+int launch_split_tc(const SplitProblem &p, int poly16, bool scalar, int grid, int *err,
+                    cudaStream_t s);
+int split_tc_occupancy(int poly16, bool scalar, int *ctas_per_sm);
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
                  int *err, cudaStream_t s);
 int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,

@@ -501,10 +501,14 @@ constexpr Variant kVariants[] = {
     {512, 4, 1024, 0, 2, 1, 1},  // 31: as 30, warp-specialised sin/cos (4 of 16 warps polynomial)
     {512, 2, 1024, 0, 2, 1, 1},  // 32: TT 1024 (tiles of 23), warp-specialised sin/cos
     // pair model 3: the phase on the tensor cores (kernel_tc.cu), TT 512, source tiles
-    // of 1024; `poly` of every 8 source pairs on the FMA-pipe sin/cos
-    {512, 1, 1024, 2, 3, 1, 0, 1},  // 33
-    {512, 1, 1024, 3, 3, 1, 0, 1},  // 34
-    {512, 1, 1024, 4, 3, 1, 0, 1},  // 35
+    // of 1024; `poly` of every 16 source pairs on the FMA-pipe sin/cos
+    {512, 1, 1024, 4, 3, 1, 0, 1},     // 33
+    {512, 1, 1024, 6, 3, 1, 0, 1},     // 34
+    {512, 1, 1024, 8, 3, 1, 0, 1},     // 35
+    {512, 1, 1024, 7, 3, 1, 0, 1},     // 36
+    {512, 1, 1024, 5, 3, 1, 0, 1},     // 37
+    {512, 1, 1024, 6, 3, 1, 0, 1, 1},  // 38: as 34, MUFU pairs accumulated unpacked
+    {512, 1, 1024, 7, 3, 1, 0, 1, 1},  // 39: as 36, MUFU pairs accumulated unpacked
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -613,7 +617,8 @@ std::vector<int> split_preferences(size_t N, size_t M) {
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
                  int *err, cudaStream_t s) {
   if (is_tc(variant)) {
-    if (!const_phase && !mc) return launch_split_tc(p, kVariants[variant].poly, grid, err, s);
+    if (!const_phase && !mc)
+      return launch_split_tc(p, kVariants[variant].poly, kVariants[variant].sc != 0, grid, err, s);
     variant = kTcFallback;
   }
 #define CALL(T, R, C, P) launch_variant<T, R, C, P>(p, grid, const_phase, mc, err, s)
@@ -631,7 +636,7 @@ int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, i
 
 int split_occupancy(int variant, bool mc, int *ctas_per_sm) {
   if (is_tc(variant)) {
-    if (!mc) return split_tc_occupancy(kVariants[variant].poly, ctas_per_sm);
+    if (!mc) return split_tc_occupancy(kVariants[variant].poly, kVariants[variant].sc != 0, ctas_per_sm);
     variant = kTcFallback;
   }
 #define CALL(T, R, C, P) occupancy_variant<T, R, C, P>(mc, ctas_per_sm)

@@ -17,8 +17,9 @@
 // TF32 parts against constant ones (exact products) in a second K block.  The
 // accumulator lives in tensor memory (two buffers of 256 columns); 16 consumer
 // warps read it with tcgen05.ld (warp w: TMEM lanes 32 (w % 4).., columns
-// 64 (w / 4)..), take sin/cos (MUFU, or the FMA-pipe polynomial for NPP of
-// every 8 source pairs) and accumulate a' e^{i theta'} on packed f32x2 pairs.
+// 64 (w / 4)..), take sin/cos (MUFU, or the FMA-pipe polynomial for NPP0 /
+// NPP1 of the 8 source pairs of even / odd 16-column chunks) and accumulate
+// a' e^{i theta'} on packed f32x2 pairs (SC: the MUFU pairs in scalar FP32).
 // One more warp allocates the tensor memory and issues the MMAs (one thread),
 // tracked by mbarriers: full[b] (tcgen05.commit) and free[b] (16 consumer
 // arrivals).  Per pair on the CUDA cores: 3 FP32-pipe ops + 2 MUFU ops.
@@ -90,7 +91,7 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
   return false;
 }
 
-template <int NPP>
+template <int NPP0, int NPP1, bool SC>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_split_tc(const SplitProblem P, int n_items, int *err) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -281,6 +282,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int lg = warp & 3, cg = warp >> 2;
         for (int m = 0; m < 4; ++m) {
           uint64_t re2 = 0ull, im2 = 0ull;
+          float res[2] = {0.f, 0.f}, ims[2] = {0.f, 0.f};  // SC: the MUFU pairs
           for (int n = 0; n < 4; ++n) {
             const int b = (m * 4 + n) & 1;
             const bool ok =
@@ -309,14 +311,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                   av[4 * q + 3] = v.w;
                 }
                 const uint32_t *th = rv[ch & 1];
+                const int npp = (ch & 1) ? NPP1 : NPP0;
 #pragma unroll
                 for (int pp = 0; pp < 8; ++pp) {
                   const float t0 = __uint_as_float(th[2 * pp]);
                   const float t1 = __uint_as_float(th[2 * pp + 1]);
+                  if (SC && pp >= npp) {
+                    // XU pipe, scalar accumulation (no packing of the MUFU results)
+                    res[0] = fmaf(av[2 * pp], ptx::cos_approx(t0), res[0]);
+                    ims[0] = fmaf(av[2 * pp], ptx::sin_approx(t0), ims[0]);
+                    res[1] = fmaf(av[2 * pp + 1], ptx::cos_approx(t1), res[1]);
+                    ims[1] = fmaf(av[2 * pp + 1], ptx::sin_approx(t1), ims[1]);
+                    continue;
+                  }
                   const uint64_t t2 = ptx::pack2(t0, t1);
                   const uint64_t am = ptx::pack2(av[2 * pp], av[2 * pp + 1]);
                   uint64_t sn, cs;
-                  if (pp < NPP) {
+                  if (pp < npp) {
                     poly_sincos2(t2, sn, cs);  // FMA pipe
                   } else {
                     sn = ptx::pack2(ptx::sin_approx(t0), ptx::sin_approx(t1));  // XU pipe
@@ -334,9 +345,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           float x, y;
           ptx::unpack2(re2, x, y);
-          const float re = x + y;
+          const float re = (x + y) + (res[0] + res[1]);
           ptx::unpack2(im2, x, y);
-          part[cg * kTcTT + m * kTcM + 32 * lg + lane] = make_float2(re, x + y);
+          part[cg * kTcTT + m * kTcM + 32 * lg + lane] =
+              make_float2(re, (x + y) + (ims[0] + ims[1]));
         }
       }
       __syncthreads();  // partial sums complete
@@ -382,9 +394,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (producer) ptx::tmem_dealloc(tbase, kTcCols);
 }
 
-template <int NPP>
+template <int NPP0, int NPP1, bool SC>
 int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
-  auto kern = k_split_tc<NPP>;
+  auto kern = k_split_tc<NPP0, NPP1, SC>;
   HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)TcSmem::bytes));
   const int n_items = p.n_ttiles * p.splits;
@@ -395,33 +407,42 @@ int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
   return HOLO_OK;
 }
 
-template <int NPP>
+template <int NPP0, int NPP1, bool SC>
 int occupancy_tc(int *out) {
-  auto kern = k_split_tc<NPP>;
+  auto kern = k_split_tc<NPP0, NPP1, SC>;
   HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)TcSmem::bytes));
   HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, kTcThreads, TcSmem::bytes));
   return HOLO_OK;
 }
 
+// builds: polynomial pairs per 16 (even chunk + odd chunk), scalar MUFU accumulation
+#define HOLO_TC_DISPATCH(NP16, SCAL, CALL)                                             \
+  switch ((NP16) * 2 + ((SCAL) ? 1 : 0)) {                                             \
+    case 8: return CALL(2, 2, false);                                                  \
+    case 10: return CALL(2, 3, false);                                                 \
+    case 12: return CALL(3, 3, false);                                                 \
+    case 13: return CALL(3, 3, true);                                                  \
+    case 14: return CALL(3, 4, false);                                                 \
+    case 15: return CALL(3, 4, true);                                                  \
+    case 16: return CALL(4, 4, false);                                                 \
+    default:                                                                           \
+      return fail(HOLO_ERR_INVALID, "tensor-core split kernel: no build for %d of 16", NP16); \
+  }
+
 }  // namespace
 
-int launch_split_tc(const SplitProblem &p, int npp, int grid, int *err, cudaStream_t s) {
-  switch (npp) {
-    case 2: return launch_tc<2>(p, grid, err, s);
-    case 3: return launch_tc<3>(p, grid, err, s);
-    case 4: return launch_tc<4>(p, grid, err, s);
-    default: return fail(HOLO_ERR_INVALID, "tensor-core split kernel: no build for %d of 8", npp);
-  }
+int launch_split_tc(const SplitProblem &p, int poly16, bool scalar, int grid, int *err,
+                    cudaStream_t s) {
+#define CALL(A, B, C) launch_tc<A, B, C>(p, grid, err, s)
+  HOLO_TC_DISPATCH(poly16, scalar, CALL)
+#undef CALL
 }
 
-int split_tc_occupancy(int npp, int *ctas_per_sm) {
-  switch (npp) {
-    case 2: return occupancy_tc<2>(ctas_per_sm);
-    case 3: return occupancy_tc<3>(ctas_per_sm);
-    case 4: return occupancy_tc<4>(ctas_per_sm);
-    default: return fail(HOLO_ERR_INVALID, "tensor-core split kernel: no build for %d of 8", npp);
-  }
+int split_tc_occupancy(int poly16, bool scalar, int *ctas_per_sm) {
+#define CALL(A, B, C) occupancy_tc<A, B, C>(ctas_per_sm)
+  HOLO_TC_DISPATCH(poly16, scalar, CALL)
+#undef CALL
 }
 
 }  // namespace holo

@@ -196,13 +196,15 @@ int holo_transform_batched(holo_handle h, const holo_problem *problems, int n_pr
  * per thread whose sin/cos run on the FMA pipe, pair model).  The pair model of
  * a HOLO_SPLIT32 variant says how the curvature term and 1/r are formed per
  * pair: 0 = with the curvature correction c^2/8r^3, 1 = without it, 2 = without
- * it and with 1/r replaced by a first-order series of 1/q (no rsqrt); it is 0
+ * it and with 1/r replaced by a first-order series of 1/q (no rsqrt), 3 = model
+ * 2 with the phase computed on the tensor cores (tcgen05 TF32 MMAs); it is 0
  * for every HOLO_FP64 variant.  The pair loop is 0 for scalar FP32, 1 for
  * packed FP32 pairs (f32x2, two sources per instruction), 2 for packed pairs
  * with warp-specialised sin/cos (a quarter of the warps on the FMA-pipe
- * polynomial for all their targets; fma_sincos_targets is then 0).  The
- * planner picks one tile shape per size
- * bucket, then the cheapest pair model whose error bound holds for the point
+ * polynomial for all their targets; fma_sincos_targets is then 0), 3 for the
+ * tensor-core kernel (fma_sincos_targets then counts source pairs of every
+ * 16 on the polynomial).  The planner takes the first of a speed-ordered list
+ * of variants whose error bound holds for the point
  * sets; holo_autotune times every variant on a synthetic problem of the given
  * size and records the fastest for its bucket.  The Python layer persists the
  * table as JSON. */
