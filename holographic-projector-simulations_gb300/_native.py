@@ -80,6 +80,7 @@ SIGNATURES = {
     "holo_profile_begin": (_i, [_vp]),
     "holo_profile_end": (_i, [_vp, _c.POINTER(_d), _c.POINTER(_i)]),
     "holo_probe_peak": (_i, [_vp, _i, _c.POINTER(_d)]),
+    "holo_selftest_bounded_wait": (_i, [_vp, _c.c_longlong, _vp]),
     "holo_transform_noalloc": (_i, [_i, _i, _d, _dp, _dp, _dp, _sz, _dp, _sz, _dp, _vp]),
 }
 

@@ -84,6 +84,15 @@ __global__ void __launch_bounds__(256) k_probe_ffma2(float *out, int iters, floa
   if (s == 12345.f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// One thread waits, bounded, on a barrier phase that nothing completes: the
+// timeout path of every pipelined kernel here (raise the error word, return).
+__global__ void k_selftest_wait(long long max_cycles, int *err) {
+  __shared__ __align__(8) uint64_t bar;
+  ptx::mbar_init(&bar, 1);
+  ptx::fence_barrier_init();
+  if (!ptx::mbar_wait_bounded(&bar, 0u, max_cycles)) atomicExch(err, kDevErrTimeout);
+}
+
 }  // namespace
 }  // namespace holo
 
@@ -125,6 +134,21 @@ int holo_profile_end(holo_handle h, double *total_ms, int *launches) {
   if (launches) *launches = (int)h->prof.size();
   h->prof.clear();
   if (total_ms) *total_ms = total;
+  return HOLO_OK;
+}
+
+int holo_selftest_bounded_wait(holo_handle h, long long max_cycles, holo_stream_t stream) {
+  if (!h) return fail(HOLO_ERR_INVALID, "null handle");
+  if (max_cycles <= 0 || max_cycles > kWaitCycles)
+    return fail(HOLO_ERR_INVALID, "max_cycles must be in (0, %lld]", kWaitCycles);
+  std::lock_guard<std::mutex> lk(h->mu);
+  int prev = -1;
+  cudaGetDevice(&prev);
+  cudaSetDevice(h->device);
+  k_selftest_wait<<<1, 1, 0, (cudaStream_t)stream>>>(max_cycles, h->dev_err);
+  const cudaError_t e = cudaGetLastError();
+  if (prev >= 0) cudaSetDevice(prev);
+  if (e != cudaSuccess) return cuda_fail(e, "self-test kernel", __FILE__, __LINE__);
   return HOLO_OK;
 }
 

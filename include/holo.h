@@ -231,6 +231,13 @@ int holo_kernel_launches(long long *out);
 int holo_profile_begin(holo_handle h);
 int holo_profile_end(holo_handle h, double *total_ms, int *launches);
 int holo_probe_peak(holo_handle h, int kind, double *ops_per_s);
+/* No counterpart in the reference: a test of the failure path.  Launches one
+ * thread that waits on a barrier phase nothing completes, giving up after
+ * `max_cycles` (at most ~2 s of SM clock) exactly as the pipelined kernels do:
+ * the handle's device error word is raised, so the next holo_device_status on
+ * `stream` returns HOLO_ERR_TIMEOUT (and clears it) while the context stays
+ * usable.  No GPU fault is involved. */
+int holo_selftest_bounded_wait(holo_handle h, long long max_cycles, holo_stream_t stream);
 
 /* ---- transform without any device allocation ------------------------------
  * No counterpart in the reference: an addition for callers that cannot

@@ -297,3 +297,23 @@ def test_cli_rejects_bad_files(holo, tmp_path):
     holo.io.write_inputs(str(tmp_path), [1.0, 2.0], [0.0], [0, 0, 1, 0, 0, 1], [0, 0, 0])
     r = subprocess.run([_cli(holo), "-f", str(tmp_path)], capture_output=True, text=True)
     assert r.returncode == 2 and "inconsistent" in r.stderr
+
+
+# ---- failure path: a bounded device wait that runs out -----------------------------------
+def test_bounded_wait_timeout_is_reported_and_the_context_survives(holo, orc):
+    """A wait on a barrier that nothing completes gives up after ~1 ms of SM clock, raises
+    the handle's error word (HOLO_ERR_TIMEOUT on the next status check, then cleared), and
+    the same handle computes correctly afterwards -- no GPU fault is involved."""
+    lib, h = holo._native.load(), holo.handle(0)
+    h.status()  # nothing pending
+    assert lib.holo_selftest_bounded_wait(h.h, 2_000_000, None) == 0
+    rc = lib.holo_device_status(h.h, None)
+    assert rc == holo._native.ERR_TIMEOUT, rc
+    assert b"ran out" in lib.holo_last_error_string()
+    assert lib.holo_device_status(h.h, None) == 0  # cleared by the report
+    assert lib.holo_selftest_bounded_wait(h.h, 0, None) == holo._native.ERR_INVALID
+    amp, phase, u, v, _ = config1(seed=4)
+    u, amp, phase, v = u[:1024], amp[:1024], phase[:1024], v[:4096]
+    for prec, tol in (("fp64", 1e-12), ("split32", 1e-5)):
+        y = holo.transform(amp, phase, u, v, -1, LAM, precision=prec)
+        assert rel_l2(y, orc.transform(amp, phase, u, v, -1, LAM)) < tol
