@@ -313,8 +313,9 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
   }
 
   if (precision == HOLO_SPLIT32) {
-    // sort once; pad sources to a multiple of every source tile size
-    p->n_pad = std::max<int>(1, (int)((N + 1023) / 1024)) * 1024;
+    // sort once; pad sources to a multiple of every source tile size (3072 =
+    // lcm of 1024 and 768; the others divide 1024)
+    p->n_pad = std::max<int>(1, (int)((N + 3071) / 3072)) * 3072;
     HOLO_TRY(sort_set(p.get(), u, (int)N, p->n_pad, &p->pos_s, &p->order_s, s));
     HOLO_TRY(sort_set(p.get(), v, (int)M, (int)M, &p->pos_t, &p->order_t, s));
     HOLO_TRY(alloc_plan(p.get(), (void **)&p->tiles_s, (size_t)6 * (N / 256 + 1) * sizeof(double), s));

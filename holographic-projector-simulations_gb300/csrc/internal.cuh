@@ -169,11 +169,12 @@ int launch_gather_apf(const double *amp, const double *phase, const int32_t *ord
                       int n_pad, float2 *out, cudaStream_t s);
 
 // kernel_split.cu
-// kernel_tc.cu: the tensor-core split kernel (pair model 3), `poly16` of every 16
-// source pairs on the FMA-pipe sin/cos, `scalar`: MUFU pairs accumulated unpacked
-int launch_split_tc(const SplitProblem &p, int poly16, bool scalar, int grid, int *err,
-                    cudaStream_t s);
-int split_tc_occupancy(int poly16, bool scalar, int *ctas_per_sm);
+// kernel_tc.cu: the tensor-core split kernel (pair model 3) with `groups` (4 or 6)
+// consumer warps per TMEM lane group (source tiles of 1024 or 768), `poly16` of every
+// 16 source pairs on the FMA-pipe sin/cos, `scalar`: MUFU pairs accumulated unpacked
+int launch_split_tc(const SplitProblem &p, int groups, int poly16, bool scalar, int grid,
+                    int *err, cudaStream_t s);
+int split_tc_occupancy(int groups, int poly16, bool scalar, int *ctas_per_sm);
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
                  int *err, cudaStream_t s);
 int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,

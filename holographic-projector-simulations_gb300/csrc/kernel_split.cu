@@ -509,6 +509,11 @@ constexpr Variant kVariants[] = {
     {512, 1, 1024, 5, 3, 1, 0, 1},     // 37
     {512, 1, 1024, 6, 3, 1, 0, 1, 1},  // 38: as 34, MUFU pairs accumulated unpacked
     {512, 1, 1024, 7, 3, 1, 0, 1, 1},  // 39: as 36, MUFU pairs accumulated unpacked
+    {128, 4, 768, 1, 2, 1},            // 40: packed model 2, TT 512 x source tiles of 768
+    // pair model 3 with 24 consumer warps (6 per TMEM lane group), source tiles of 768
+    {512, 1, 768, 6, 3, 1, 0, 1},      // 41
+    {512, 1, 768, 5, 3, 1, 0, 1},      // 42
+    {512, 1, 768, 7, 3, 1, 0, 1},      // 43
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -562,11 +567,13 @@ int split_variant_count() { return kNumVariants; }
 Variant split_variant(int i) { return kVariants[i]; }
 
 // The tensor-core variants have no Monte Carlo, constant-phase or batched build:
-// those calls run variant 26, which has the same tiles (512 targets, 1024 sources).
-constexpr int kTcFallback = 26;
+// those calls run a CUDA-core variant with the same tiles (512 targets and 1024 or
+// 768 sources: variant 26 or 40).
 static bool is_tc(int v) { return v >= 0 && v < kNumVariants && kVariants[v].tc; }
+static int tc_fallback(int v) { return kVariants[v].cs == 768 ? 40 : 26; }
+static int tc_groups(int v) { return kVariants[v].cs == 768 ? 6 : 4; }
 
-int split_batched_variant(int v) { return is_tc(v) ? kTcFallback : v; }
+int split_batched_variant(int v) { return is_tc(v) ? tc_fallback(v) : v; }
 
 std::vector<int> split_preferences(size_t N, size_t M) {
   (void)N;
@@ -608,6 +615,7 @@ std::vector<int> split_preferences(size_t N, size_t M) {
     case 27: return CALL(256, 4, 512, 1 | 96);            \
     case 28: return CALL(256, 4, 512, 0 | 96);            \
     case 29: return CALL(128, 4, 512, 1 | 96);            \
+    case 40: return CALL(128, 4, 768, 1 | 96);            \
     case 30: return CALL(512, 4, 1024, 1 | 96);           \
     case 31: return CALL(512, 4, 1024, 0 | 96 | 128);     \
     case 32: return CALL(512, 2, 1024, 0 | 96 | 128);     \
@@ -618,8 +626,9 @@ int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase,
                  int *err, cudaStream_t s) {
   if (is_tc(variant)) {
     if (!const_phase && !mc)
-      return launch_split_tc(p, kVariants[variant].poly, kVariants[variant].sc != 0, grid, err, s);
-    variant = kTcFallback;
+      return launch_split_tc(p, tc_groups(variant), kVariants[variant].poly,
+                             kVariants[variant].sc != 0, grid, err, s);
+    variant = tc_fallback(variant);
   }
 #define CALL(T, R, C, P) launch_variant<T, R, C, P>(p, grid, const_phase, mc, err, s)
   HOLO_SPLIT_DISPATCH(variant, CALL)
@@ -628,7 +637,7 @@ int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase,
 
 int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,
                          int *queue, int variant, int grid, int *err, cudaStream_t s) {
-  if (is_tc(variant)) variant = kTcFallback;
+  if (is_tc(variant)) variant = tc_fallback(variant);
 #define CALL(T, R, C, P) batched_variant<T, R, C, P>(probs_dev, items, n_items, queue, grid, err, s)
   HOLO_SPLIT_DISPATCH(variant, CALL)
 #undef CALL
@@ -636,8 +645,10 @@ int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, i
 
 int split_occupancy(int variant, bool mc, int *ctas_per_sm) {
   if (is_tc(variant)) {
-    if (!mc) return split_tc_occupancy(kVariants[variant].poly, kVariants[variant].sc != 0, ctas_per_sm);
-    variant = kTcFallback;
+    if (!mc)
+      return split_tc_occupancy(tc_groups(variant), kVariants[variant].poly,
+                                kVariants[variant].sc != 0, ctas_per_sm);
+    variant = tc_fallback(variant);
   }
 #define CALL(T, R, C, P) occupancy_variant<T, R, C, P>(mc, ctas_per_sm)
   HOLO_SPLIT_DISPATCH(variant, CALL)

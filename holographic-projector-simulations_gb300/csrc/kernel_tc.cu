@@ -37,13 +37,24 @@ namespace {
 
 #include "split_frame.cuh"
 
-constexpr int kTcTT = 512;                    // targets per CTA
-constexpr int kTcCS = 1024;                   // sources per tile
-constexpr int kTcM = 128, kTcN = 256, kTcK = 8;
-constexpr int kTcConsumers = 16;              // consumer warps
-constexpr int kTcThreads = 32 * (kTcConsumers + 1);
-constexpr int kTcCols = 2 * kTcN;             // TMEM columns: two accumulator buffers
+constexpr int kTcTT = 512;                    // targets per CTA (4 blocks of 128)
+constexpr int kTcM = 128, kTcK = 8;
+constexpr int kTcCols = 512;                  // TMEM columns allocated: two accumulator buffers
 constexpr uint32_t kTcLbo = 128, kTcSbo = 256;  // operand layout (bytes), see tc_off
+
+// Shape of one build: CG column groups of consumer warps per TMEM lane group (4 lane
+// groups of 32 targets), NB sources per MMA block (TMEM columns per buffer), CS = 4 NB
+// sources per tile.  CG = 4: 16 consumer warps, NB 256; CG = 6: 24 warps, NB 192.
+template <int CG>
+struct TcShape {
+  static_assert(CG == 4 || CG == 6, "tensor-core split kernel: 4 or 6 column groups");
+  static constexpr int NB = CG == 4 ? 256 : 192;
+  static constexpr int CS = 4 * NB;
+  static constexpr int Consumers = 4 * CG;        // consumer warps
+  static constexpr int Threads = 32 * (Consumers + 1);
+  static constexpr int Cols = NB / CG;            // columns per consumer warp per block
+  static constexpr int Chunks = Cols / 16;        // 16-column loads per block
+};
 
 // Float offset of element (row r, feature k) of a K-major tf32 operand with K = 8:
 // core matrices of 8 rows x 4 features (16 B rows, 128 B), the two along K 128 B
@@ -53,7 +64,9 @@ __host__ __device__ __forceinline__ int tc_off(int r, int k) {
   return (r >> 3) * 64 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3);
 }
 
+template <int CG>
 struct TcSmem {
+  static constexpr int kTcCS = TcShape<CG>::CS;
   static constexpr size_t raw_geo = 0;                                 // float [CS*6]
   static constexpr size_t raw_apf = raw_geo + kTcCS * 6 * 4;           // float2 [CS]
   static constexpr size_t opb_hi = raw_apf + kTcCS * 8;                // float [CS*8]
@@ -63,8 +76,8 @@ struct TcSmem {
   static constexpr size_t opa_lo = opa_hi + kTcTT * kTcK * 4;          // float [TT*8]
   static constexpr size_t opa_one = opa_lo + kTcTT * kTcK * 4;         // float [128*8]: (1,1,1,0..)
   static constexpr size_t amp = opa_one + kTcM * kTcK * 4;             // float [CS]
-  static constexpr size_t part = amp + kTcCS * 4;                      // float2 [4][TT]
-  static constexpr size_t acc = part + 4 * kTcTT * 8;                  // double2 [TT]
+  static constexpr size_t part = amp + kTcCS * 4;                      // float2 [CG][TT]
+  static constexpr size_t acc = part + CG * kTcTT * 8;                 // double2 [TT]
   static constexpr size_t tph = acc + kTcTT * 16;                      // float [TT]
   static constexpr size_t tsc = tph + kTcTT * 4;                       // float [TT]
   static constexpr size_t frame = tsc + kTcTT * 4;                     // Frame [2]
@@ -72,8 +85,11 @@ struct TcSmem {
   static constexpr size_t misc = bars + 5 * 8;                         // uint32 taddr, abort
   static constexpr size_t bytes = misc + 16;
 };
-static_assert(TcSmem::bytes <= 227 * 1024, "tensor-core split kernel: shared memory");
-static_assert(TcSmem::opb_hi % 128 == 0 && TcSmem::opa_hi % 128 == 0 && TcSmem::opa_one % 16 == 0,
+static_assert(TcSmem<4>::bytes <= 227 * 1024 && TcSmem<6>::bytes <= 227 * 1024,
+              "tensor-core split kernel: shared memory");
+static_assert(TcSmem<4>::opb_hi % 128 == 0 && TcSmem<4>::opa_hi % 128 == 0 &&
+                  TcSmem<6>::opb_hi % 128 == 0 && TcSmem<6>::opa_hi % 128 == 0 &&
+                  TcSmem<6>::opa_one % 16 == 0 && TcSmem<6>::amp % 16 == 0,
               "operand alignment");
 
 __device__ __forceinline__ void split_range_tc(int n, int splits, int s, int *b, int *e) {
@@ -91,11 +107,14 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
   return false;
 }
 
-template <int NPP0, int NPP1, bool SC>
-__global__ void __launch_bounds__(kTcThreads, 1)
+template <int CG, int NPP0, int NPP1, bool SC>
+__global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
     k_split_tc(const SplitProblem P, int n_items, int *err) {
   extern __shared__ __align__(128) unsigned char smem[];
-  using L = TcSmem;
+  using L = TcSmem<CG>;
+  using S = TcShape<CG>;
+  constexpr int kTcCS = S::CS, kTcN = S::NB, kTcConsumers = S::Consumers;
+  constexpr int kTcThreads = S::Threads;
   float *raw_geo = reinterpret_cast<float *>(smem + L::raw_geo);
   float2 *raw_apf = reinterpret_cast<float2 *>(smem + L::raw_apf);
   float *opb_hi = reinterpret_cast<float *>(smem + L::opb_hi);
@@ -213,8 +232,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           amp[i] = am;
         }
-        // targets: one per consumer thread
-        {
+        // targets: one per consumer thread (the first kTcTT of them)
+        if (tid < kTcTT) {
           const int t = tid;
           const int ti = tt * kTcTT + t;
           float th[3] = {0.f, 0.f, 0.f}, tl[3] = {0.f, 0.f, 0.f};
@@ -292,15 +311,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (ok) {
               // the load of chunk ch + 1 is in flight while chunk ch is summed
               const uint32_t ta =
-                  tbase + ((uint32_t)(32 * lg) << 16) + (uint32_t)(b * kTcN + cg * 64);
+                  tbase + ((uint32_t)(32 * lg) << 16) + (uint32_t)(b * kTcN + cg * S::Cols);
               uint32_t rv[2][16];
               ptx::tmem_ld16_nowait(ta, rv[0]);
               ptx::tmem_wait16(rv[0]);
 #pragma unroll
-              for (int ch = 0; ch < 4; ++ch) {
-                if (ch < 3) ptx::tmem_ld16_nowait(ta + (uint32_t)(16 * (ch + 1)), rv[(ch + 1) & 1]);
+              for (int ch = 0; ch < S::Chunks; ++ch) {
+                if (ch + 1 < S::Chunks)
+                  ptx::tmem_ld16_nowait(ta + (uint32_t)(16 * (ch + 1)), rv[(ch + 1) & 1]);
                 const float4 *ap =
-                    reinterpret_cast<const float4 *>(amp + n * kTcN + cg * 64 + 16 * ch);
+                    reinterpret_cast<const float4 *>(amp + n * kTcN + cg * S::Cols + 16 * ch);
                 float av[16];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -336,7 +356,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                   re2 = ptx::fma2(am, cs, re2);
                   im2 = ptx::fma2(am, sn, im2);
                 }
-                if (ch < 3) ptx::tmem_wait16(rv[(ch + 1) & 1]);
+                if (ch + 1 < S::Chunks) ptx::tmem_wait16(rv[(ch + 1) & 1]);
               }
             }
             ptx::tc_fence_before();
@@ -353,14 +373,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       __syncthreads();  // partial sums complete
 
-      // ---- per target: sum the four column groups, scale, rotate, carry in FP64 ----
-      if (!producer) {
+      // ---- per target: sum the column groups, scale, rotate, carry in FP64 ----
+      if (tid < kTcTT) {
         const int t = tid;
-        const float2 s0 = part[t], s1 = part[kTcTT + t], s2 = part[2 * kTcTT + t],
-                     s3 = part[3 * kTcTT + t];
+        float sx = 0.f, sy = 0.f;
+#pragma unroll
+        for (int c = 0; c < CG; ++c) {
+          const float2 v = part[c * kTcTT + t];
+          sx += v.x;
+          sy += v.y;
+        }
         const float sc = tsc[t];
-        const float re = ((s0.x + s1.x) + (s2.x + s3.x)) * sc;
-        const float im = sgn * ((s0.y + s1.y) + (s2.y + s3.y)) * sc;
+        const float re = sx * sc;
+        const float im = sgn * sy * sc;
         float sr, cr;
         __sincosf(tph[t], &sr, &cr);
         double2 a = acc[t];
@@ -394,54 +419,59 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (producer) ptx::tmem_dealloc(tbase, kTcCols);
 }
 
-template <int NPP0, int NPP1, bool SC>
+template <int CG, int NPP0, int NPP1, bool SC>
 int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
-  auto kern = k_split_tc<NPP0, NPP1, SC>;
-  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)TcSmem::bytes));
+  auto kern = k_split_tc<CG, NPP0, NPP1, SC>;
+  constexpr int bytes = (int)TcSmem<CG>::bytes;
+  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   const int n_items = p.n_ttiles * p.splits;
   if (n_items <= 0) return HOLO_OK;
-  kern<<<grid, kTcThreads, TcSmem::bytes, s>>>(p, n_items, err);
+  kern<<<grid, TcShape<CG>::Threads, bytes, s>>>(p, n_items, err);
   note_launches(1);
   HOLO_CUDA(cudaGetLastError());
   return HOLO_OK;
 }
 
-template <int NPP0, int NPP1, bool SC>
+template <int CG, int NPP0, int NPP1, bool SC>
 int occupancy_tc(int *out) {
-  auto kern = k_split_tc<NPP0, NPP1, SC>;
-  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)TcSmem::bytes));
-  HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, kTcThreads, TcSmem::bytes));
+  auto kern = k_split_tc<CG, NPP0, NPP1, SC>;
+  constexpr int bytes = (int)TcSmem<CG>::bytes;
+  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, TcShape<CG>::Threads, bytes));
   return HOLO_OK;
 }
 
-// builds: polynomial pairs per 16 (even chunk + odd chunk), scalar MUFU accumulation
-#define HOLO_TC_DISPATCH(NP16, SCAL, CALL)                                             \
-  switch ((NP16) * 2 + ((SCAL) ? 1 : 0)) {                                             \
-    case 8: return CALL(2, 2, false);                                                  \
-    case 10: return CALL(2, 3, false);                                                 \
-    case 12: return CALL(3, 3, false);                                                 \
-    case 13: return CALL(3, 3, true);                                                  \
-    case 14: return CALL(3, 4, false);                                                 \
-    case 15: return CALL(3, 4, true);                                                  \
-    case 16: return CALL(4, 4, false);                                                 \
+// builds: column groups, polynomial pairs per 16 (even chunk + odd chunk), scalar
+// MUFU accumulation
+#define HOLO_TC_DISPATCH(CGS, NP16, SCAL, CALL)                                        \
+  switch ((CGS) * 100 + (NP16) * 2 + ((SCAL) ? 1 : 0)) {                               \
+    case 408: return CALL(4, 2, 2, false);                                             \
+    case 410: return CALL(4, 2, 3, false);                                             \
+    case 412: return CALL(4, 3, 3, false);                                             \
+    case 413: return CALL(4, 3, 3, true);                                              \
+    case 414: return CALL(4, 3, 4, false);                                             \
+    case 415: return CALL(4, 3, 4, true);                                              \
+    case 416: return CALL(4, 4, 4, false);                                             \
+    case 610: return CALL(6, 2, 3, false);                                             \
+    case 612: return CALL(6, 3, 3, false);                                             \
+    case 614: return CALL(6, 3, 4, false);                                             \
     default:                                                                           \
-      return fail(HOLO_ERR_INVALID, "tensor-core split kernel: no build for %d of 16", NP16); \
+      return fail(HOLO_ERR_INVALID, "tensor-core split kernel: no build for %d groups, %d of 16", \
+                  CGS, NP16);                                                          \
   }
 
 }  // namespace
 
-int launch_split_tc(const SplitProblem &p, int poly16, bool scalar, int grid, int *err,
-                    cudaStream_t s) {
-#define CALL(A, B, C) launch_tc<A, B, C>(p, grid, err, s)
-  HOLO_TC_DISPATCH(poly16, scalar, CALL)
+int launch_split_tc(const SplitProblem &p, int groups, int poly16, bool scalar, int grid,
+                    int *err, cudaStream_t s) {
+#define CALL(G, A, B, C) launch_tc<G, A, B, C>(p, grid, err, s)
+  HOLO_TC_DISPATCH(groups, poly16, scalar, CALL)
 #undef CALL
 }
 
-int split_tc_occupancy(int poly16, bool scalar, int *ctas_per_sm) {
-#define CALL(A, B, C) occupancy_tc<A, B, C>(ctas_per_sm)
-  HOLO_TC_DISPATCH(poly16, scalar, CALL)
+int split_tc_occupancy(int groups, int poly16, bool scalar, int *ctas_per_sm) {
+#define CALL(G, A, B, C) occupancy_tc<G, A, B, C>(ctas_per_sm)
+  HOLO_TC_DISPATCH(groups, poly16, scalar, CALL)
 #undef CALL
 }
 

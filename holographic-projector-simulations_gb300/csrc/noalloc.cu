@@ -153,7 +153,7 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
   }
 
   // ---- carve the array ----
-  const int n_pad = (int)((N + 1023) / 1024) * 1024;
+  const int n_pad = (int)((N + 3071) / 3072) * 3072;  // a multiple of every source tile
   Carve cv{base};
   int *err = cv.take<int>(16);
   double *stats = cv.take<double>(20);
