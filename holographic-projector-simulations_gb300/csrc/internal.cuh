@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -143,6 +144,31 @@ struct Fp64Problem {
 struct WorkItem {
   int problem, ttile, s_begin, s_end, split, pad0, pad1, pad2;
 };
+
+// ---- per-device kernel set-up ------------------------------------------------------
+// Raise Kern's dynamic shared-memory limit to `smem_bytes` and query its CTAs per SM,
+// once per device (the host API calls cost microseconds per launch); the result is
+// cached per kernel and device.  `ctas_per_sm` may be null.
+template <auto Kern>
+int kernel_setup(int threads, int smem_bytes, int *ctas_per_sm) {
+  static std::atomic<int> cache[64];  // CTAs per SM + 1 per device; 0: not set up yet
+  int dev = 0;
+  HOLO_CUDA(cudaGetDevice(&dev));
+  const bool cached = dev >= 0 && dev < 64;
+  if (cached) {
+    const int c = cache[dev].load(std::memory_order_acquire);
+    if (c > 0) {
+      if (ctas_per_sm) *ctas_per_sm = c - 1;
+      return HOLO_OK;
+    }
+  }
+  HOLO_CUDA(cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  int occ = 0;
+  HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, Kern, threads, smem_bytes));
+  if (cached) cache[dev].store(occ + 1, std::memory_order_release);
+  if (ctas_per_sm) *ctas_per_sm = occ;
+  return HOLO_OK;
+}
 
 // ---- launchers (defined in the .cu files) --------------------------------------
 // probe.cu: count of kernels this library launched (reported by the benchmark)

@@ -139,13 +139,11 @@ int launch_variant(const Fp64Problem &p, int grid, bool cst, int *err, cudaStrea
   if (n_items <= 0) return HOLO_OK;
   if (cst) {
     auto kern = k_fp64<THREADS, R, CS, true>;
-    HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)L::bytes));
+    HOLO_TRY((kernel_setup<k_fp64<THREADS, R, CS, true>>(THREADS, (int)L::bytes, nullptr)));
     kern<<<grid, THREADS, L::bytes, s>>>(p, n_items, err); note_launches(1);
   } else {
     auto kern = k_fp64<THREADS, R, CS, false>;
-    HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)L::bytes));
+    HOLO_TRY((kernel_setup<k_fp64<THREADS, R, CS, false>>(THREADS, (int)L::bytes, nullptr)));
     kern<<<grid, THREADS, L::bytes, s>>>(p, n_items, err); note_launches(1);
   }
   HOLO_CUDA(cudaGetLastError());
@@ -155,11 +153,7 @@ int launch_variant(const Fp64Problem &p, int grid, bool cst, int *err, cudaStrea
 template <int THREADS, int R, int CS>
 int occupancy_variant(int *out) {
   using L = Fp64Smem<THREADS, R, CS>;
-  auto kern = k_fp64<THREADS, R, CS, false>;
-  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)L::bytes));
-  HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, THREADS, L::bytes));
-  return HOLO_OK;
+  return kernel_setup<k_fp64<THREADS, R, CS, false>>(THREADS, (int)L::bytes, out);
 }
 
 }  // namespace

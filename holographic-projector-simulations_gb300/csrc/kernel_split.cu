@@ -521,8 +521,8 @@ template <int THREADS, int R, int CS, int POLY, bool CONST, bool MC>
 int launch_one(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
   using L = SplitSmem<THREADS, R, CS>;
   auto kern = k_split<THREADS, R, CS, POLY, CONST, MC>;
-  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)L::bytes));
+  HOLO_TRY((kernel_setup<k_split<THREADS, R, CS, POLY, CONST, MC>>(THREADS, (int)L::bytes,
+                                                                   nullptr)));
   const int n_items = p.n_ttiles * p.splits;
   if (n_items <= 0) return HOLO_OK;
   kern<<<grid, THREADS, L::bytes, s>>>(p, n_items, err); note_launches(1);
@@ -544,8 +544,7 @@ int batched_variant(const SplitProblem *probs, const WorkItem *items, int n_item
                     int grid, int *err, cudaStream_t s) {
   using L = SplitSmem<THREADS, R, CS>;
   auto kern = k_split_batched<THREADS, R, CS, POLY>;
-  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)L::bytes));
+  HOLO_TRY((kernel_setup<k_split_batched<THREADS, R, CS, POLY>>(THREADS, (int)L::bytes, nullptr)));
   kern<<<grid, THREADS, L::bytes, s>>>(probs, items, n_items, queue, err); note_launches(1);
   HOLO_CUDA(cudaGetLastError());
   return HOLO_OK;
@@ -554,11 +553,8 @@ int batched_variant(const SplitProblem *probs, const WorkItem *items, int n_item
 template <int THREADS, int R, int CS, int POLY>
 int occupancy_variant(bool mc, int *out) {
   using L = SplitSmem<THREADS, R, CS>;
-  auto kern = mc ? k_split<THREADS, R, CS, POLY, false, true> : k_split<THREADS, R, CS, POLY, false, false>;
-  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)L::bytes));
-  HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, THREADS, L::bytes));
-  return HOLO_OK;
+  if (mc) return kernel_setup<k_split<THREADS, R, CS, POLY, false, true>>(THREADS, (int)L::bytes, out);
+  return kernel_setup<k_split<THREADS, R, CS, POLY, false, false>>(THREADS, (int)L::bytes, out);
 }
 
 }  // namespace

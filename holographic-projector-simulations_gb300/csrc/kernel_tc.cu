@@ -423,7 +423,7 @@ template <int CG, int NPP0, int NPP1, bool SC>
 int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
   auto kern = k_split_tc<CG, NPP0, NPP1, SC>;
   constexpr int bytes = (int)TcSmem<CG>::bytes;
-  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  HOLO_TRY((kernel_setup<k_split_tc<CG, NPP0, NPP1, SC>>(TcShape<CG>::Threads, bytes, nullptr)));
   const int n_items = p.n_ttiles * p.splits;
   if (n_items <= 0) return HOLO_OK;
   kern<<<grid, TcShape<CG>::Threads, bytes, s>>>(p, n_items, err);
@@ -434,11 +434,8 @@ int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
 
 template <int CG, int NPP0, int NPP1, bool SC>
 int occupancy_tc(int *out) {
-  auto kern = k_split_tc<CG, NPP0, NPP1, SC>;
   constexpr int bytes = (int)TcSmem<CG>::bytes;
-  HOLO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  HOLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, TcShape<CG>::Threads, bytes));
-  return HOLO_OK;
+  return kernel_setup<k_split_tc<CG, NPP0, NPP1, SC>>(TcShape<CG>::Threads, bytes, out);
 }
 
 // builds: column groups, polynomial pairs per 16 (even chunk + odd chunk), scalar
