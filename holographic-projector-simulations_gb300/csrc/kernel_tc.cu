@@ -97,6 +97,23 @@ __device__ __forceinline__ void split_range_tc(int n, int splits, int s, int *b,
   *e = (int)(((long long)n * (s + 1)) / splits);
 }
 
+// Row r of an operand pair (hi, lo): the 8 features split into TF32 high parts and
+// TF32 remainders, written as four 16-byte stores (features 0-3 and 4-7 of a row
+// are contiguous; eight consecutive rows fill 128 bytes, so a warp's stores are
+// free of bank conflicts).
+__device__ __forceinline__ void store_row_split(float *hi, float *lo, int r, const float *x) {
+  float h[kTcK], l[kTcK];
+#pragma unroll
+  for (int k = 0; k < kTcK; ++k) {
+    h[k] = ptx::to_tf32(x[k]);
+    l[k] = ptx::to_tf32(__fsub_rn(x[k], h[k]));
+  }
+  *reinterpret_cast<float4 *>(hi + tc_off(r, 0)) = make_float4(h[0], h[1], h[2], h[3]);
+  *reinterpret_cast<float4 *>(hi + tc_off(r, 4)) = make_float4(h[4], h[5], h[6], h[7]);
+  *reinterpret_cast<float4 *>(lo + tc_off(r, 0)) = make_float4(l[0], l[1], l[2], l[3]);
+  *reinterpret_cast<float4 *>(lo + tc_off(r, 4)) = make_float4(l[4], l[5], l[6], l[7]);
+}
+
 // Bounded wait that gives up at once when the CTA has aborted.
 __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
                                         int *err) {
@@ -223,13 +240,10 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
             a3[2] = ptx::to_tf32(__fsub_rn(r1, a3[1]));
             am = pa.y * fmaf(Ps, ir0, 1.f);
           }
-#pragma unroll
-          for (int k = 0; k < kTcK; ++k) {
-            const float hi = ptx::to_tf32(g[k]);
-            opb_hi[tc_off(i, k)] = hi;
-            opb_lo[tc_off(i, k)] = ptx::to_tf32(__fsub_rn(g[k], hi));
-            opb_a[tc_off(i, k)] = k < 3 ? a3[k] : 0.f;
-          }
+          store_row_split(opb_hi, opb_lo, i, g);
+          const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+          *reinterpret_cast<float4 *>(opb_a + tc_off(i, 0)) = make_float4(a3[0], a3[1], a3[2], 0.f);
+          *reinterpret_cast<float4 *>(opb_a + tc_off(i, 4)) = z;
           amp[i] = am;
         }
         // targets: one per consumer thread (the first kTcTT of them)
@@ -253,12 +267,7 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
           const float Iq = ak / Qt, Kq = Iq / Qt;
           const float f[kTcK] = {Iq, -2.f * Iq * Tx, -2.f * Iq * Ty, Kq * T2,
                                  Kq, -2.f * Kq * Tx, -2.f * Kq * Ty, 0.f};
-#pragma unroll
-          for (int k = 0; k < kTcK; ++k) {
-            const float hi = ptx::to_tf32(f[k]);
-            opa_hi[tc_off(t, k)] = hi;
-            opa_lo[tc_off(t, k)] = ptx::to_tf32(__fsub_rn(f[k], hi));
-          }
+          store_row_split(opa_hi, opa_lo, t, f);
           tph[t] = B + sgn * Iq * T2;  // the target's rotation, incl. the Iq T2 term
           tsc[t] = Iq * iak;           // 1 / Qt
         }
