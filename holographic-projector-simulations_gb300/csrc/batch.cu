@@ -91,7 +91,7 @@ int batch_build(holo_batch_s *b, const holo_problem *pr, int n, int precision, c
   std::vector<int> group_of(n);
   for (int i = 0; i < n; ++i) {
     size_t g = 0;
-    const int v = split_batched_variant(b->plans[i]->variant);
+    const int v = b->plans[i]->variant;
     while (g < groups.size() && groups[g].variant != v) ++g;
     if (g == groups.size()) {
       groups.emplace_back();

@@ -77,8 +77,6 @@ int split_variant_count();
 Variant split_variant(int i);
 // Split variants in the planner's order of preference (fastest first) for N x M.
 std::vector<int> split_preferences(size_t N, size_t M);
-// The variant a batched (work-queue) launch runs for a plan of variant v.
-int split_batched_variant(int v);
 
 // Largest tile boxes of a source and a target tiling: per set the bounding box
 // of all tiles (lo, hi), the largest tile half-diagonal h and the largest
@@ -201,6 +199,9 @@ int launch_gather_apf(const double *amp, const double *phase, const int32_t *ord
 int launch_split_tc(const SplitProblem &p, int groups, int poly16, bool scalar, int grid,
                     int *err, cudaStream_t s);
 int split_tc_occupancy(int groups, int poly16, bool scalar, int *ctas_per_sm);
+int launch_split_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items,
+                            int *queue, int groups, int poly16, bool scalar, int grid, int *err,
+                            cudaStream_t s);
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
                  int *err, cudaStream_t s);
 int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,

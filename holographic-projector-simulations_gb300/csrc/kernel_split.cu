@@ -562,14 +562,12 @@ int occupancy_variant(bool mc, int *out) {
 int split_variant_count() { return kNumVariants; }
 Variant split_variant(int i) { return kVariants[i]; }
 
-// The tensor-core variants have no Monte Carlo, constant-phase or batched build:
-// those calls run a CUDA-core variant with the same tiles (512 targets and 1024 or
-// 768 sources: variant 26 or 40).
+// The tensor-core variants have no Monte Carlo or constant-phase build: those
+// calls run a CUDA-core variant with the same tiles (512 targets and 1024 or 768
+// sources: variant 26 or 40).
 static bool is_tc(int v) { return v >= 0 && v < kNumVariants && kVariants[v].tc; }
 static int tc_fallback(int v) { return kVariants[v].cs == 768 ? 40 : 26; }
 static int tc_groups(int v) { return kVariants[v].cs == 768 ? 6 : 4; }
-
-int split_batched_variant(int v) { return is_tc(v) ? tc_fallback(v) : v; }
 
 std::vector<int> split_preferences(size_t N, size_t M) {
   (void)N;
@@ -633,7 +631,10 @@ int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase,
 
 int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,
                          int *queue, int variant, int grid, int *err, cudaStream_t s) {
-  if (is_tc(variant)) variant = tc_fallback(variant);
+  if (is_tc(variant))
+    return launch_split_tc_batched(probs_dev, items, n_items, queue, tc_groups(variant),
+                                   kVariants[variant].poly, kVariants[variant].sc != 0, grid, err,
+                                   s);
 #define CALL(T, R, C, P) batched_variant<T, R, C, P>(probs_dev, items, n_items, queue, grid, err, s)
   HOLO_SPLIT_DISPATCH(variant, CALL)
 #undef CALL

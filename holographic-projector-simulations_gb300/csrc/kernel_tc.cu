@@ -124,9 +124,13 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
   return false;
 }
 
-template <int CG, int NPP0, int NPP1, bool SC>
+// BATCHED: work items (problem, target tile, source range, split) come from a
+// device queue (atomic counter) and each names its own problem descriptor;
+// otherwise item i of problem P0 is target tile i / splits, split i % splits.
+template <int CG, int NPP0, int NPP1, bool SC, bool BATCHED>
 __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
-    k_split_tc(const SplitProblem P, int n_items, int *err) {
+    k_split_tc(const SplitProblem P0, const SplitProblem *__restrict__ probs,
+               const WorkItem *__restrict__ items, int n_items, int *queue, int *err) {
   extern __shared__ __align__(128) unsigned char smem[];
   using L = TcSmem<CG>;
   using S = TcShape<CG>;
@@ -173,24 +177,44 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
   ptx::tc_fence_after();
   const uint32_t tbase = *taddr_slot;
 
-  const double sk = P.sk;
-  const float kap2 = (float)(0.5 * sk), ak = fabsf(kap2), iak = 1.f / fabsf(kap2);
-  const float sgn = kap2 < 0.f ? -1.f : 1.f;
   constexpr uint32_t idesc = ptx::tc_idesc_tf32(kTcM, kTcN);
   uint32_t par_tma = 0;
   // producer: MMA groups issued per TMEM buffer; consumers: completions consumed
   uint32_t uses[2] = {0u, 0u};
+  __shared__ int s_item;
 
-  auto issue = [&](int j) {
-    ptx::mbar_arrive_expect_tx(bar_tma, kTcCS * (6 * sizeof(float) + sizeof(float2)));
-    ptx::bulk_g2s(raw_geo, P.geo_s + (size_t)j * kTcCS * 6, kTcCS * 6 * sizeof(float), bar_tma);
-    ptx::bulk_g2s(raw_apf, P.apf_s + (size_t)j * kTcCS, kTcCS * sizeof(float2), bar_tma);
-  };
-
-  for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
-    const int tt = item / P.splits, split = item % P.splits;
-    int sb, se;
-    split_range_tc(P.n_stiles, P.splits, split, &sb, &se);
+  for (int it = 0;; ++it) {
+    int item;
+    if (BATCHED) {
+      if (tid == 0) s_item = atomicAdd(queue, 1);
+      __syncthreads();
+      item = s_item;
+      __syncthreads();  // s_item is rewritten for the next item
+    } else {
+      item = blockIdx.x + it * gridDim.x;
+    }
+    if (item >= n_items) break;
+    const SplitProblem &P = BATCHED ? probs[items[item].problem] : P0;
+    int tt, split, sb, se;
+    if (BATCHED) {
+      const WorkItem w = items[item];
+      tt = w.ttile;
+      split = w.split;
+      sb = w.s_begin;
+      se = w.s_end;
+    } else {
+      tt = item / P.splits;
+      split = item % P.splits;
+      split_range_tc(P.n_stiles, P.splits, split, &sb, &se);
+    }
+    const double sk = P.sk;
+    const float kap2 = (float)(0.5 * sk), ak = fabsf(kap2), iak = 1.f / fabsf(kap2);
+    const float sgn = kap2 < 0.f ? -1.f : 1.f;
+    auto issue = [&](int j) {
+      ptx::mbar_arrive_expect_tx(bar_tma, kTcCS * (6 * sizeof(float) + sizeof(float2)));
+      ptx::bulk_g2s(raw_geo, P.geo_s + (size_t)j * kTcCS * 6, kTcCS * 6 * sizeof(float), bar_tma);
+      ptx::bulk_g2s(raw_apf, P.apf_s + (size_t)j * kTcCS, kTcCS * sizeof(float2), bar_tma);
+    };
     for (int t = tid; t < kTcTT; t += kTcThreads) acc[t] = make_double2(0.0, 0.0);
     if (tid == 0 && sb < se && !*abort_flag) issue(sb);
 
@@ -430,12 +454,27 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
 
 template <int CG, int NPP0, int NPP1, bool SC>
 int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
-  auto kern = k_split_tc<CG, NPP0, NPP1, SC>;
+  auto kern = k_split_tc<CG, NPP0, NPP1, SC, false>;
   constexpr int bytes = (int)TcSmem<CG>::bytes;
-  HOLO_TRY((kernel_setup<k_split_tc<CG, NPP0, NPP1, SC>>(TcShape<CG>::Threads, bytes, nullptr)));
+  HOLO_TRY((kernel_setup<k_split_tc<CG, NPP0, NPP1, SC, false>>(TcShape<CG>::Threads, bytes,
+                                                                 nullptr)));
   const int n_items = p.n_ttiles * p.splits;
   if (n_items <= 0) return HOLO_OK;
-  kern<<<grid, TcShape<CG>::Threads, bytes, s>>>(p, n_items, err);
+  kern<<<grid, TcShape<CG>::Threads, bytes, s>>>(p, nullptr, nullptr, n_items, nullptr, err);
+  note_launches(1);
+  HOLO_CUDA(cudaGetLastError());
+  return HOLO_OK;
+}
+
+template <int CG, int NPP0, int NPP1, bool SC>
+int launch_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items, int *queue,
+                      int grid, int *err, cudaStream_t s) {
+  auto kern = k_split_tc<CG, NPP0, NPP1, SC, true>;
+  constexpr int bytes = (int)TcSmem<CG>::bytes;
+  HOLO_TRY((kernel_setup<k_split_tc<CG, NPP0, NPP1, SC, true>>(TcShape<CG>::Threads, bytes,
+                                                                nullptr)));
+  kern<<<grid, TcShape<CG>::Threads, bytes, s>>>(SplitProblem{}, probs, items, n_items, queue,
+                                                 err);
   note_launches(1);
   HOLO_CUDA(cudaGetLastError());
   return HOLO_OK;
@@ -444,7 +483,7 @@ int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
 template <int CG, int NPP0, int NPP1, bool SC>
 int occupancy_tc(int *out) {
   constexpr int bytes = (int)TcSmem<CG>::bytes;
-  return kernel_setup<k_split_tc<CG, NPP0, NPP1, SC>>(TcShape<CG>::Threads, bytes, out);
+  return kernel_setup<k_split_tc<CG, NPP0, NPP1, SC, false>>(TcShape<CG>::Threads, bytes, out);
 }
 
 // builds: column groups, polynomial pairs per 16 (even chunk + odd chunk), scalar
@@ -471,6 +510,14 @@ int occupancy_tc(int *out) {
 int launch_split_tc(const SplitProblem &p, int groups, int poly16, bool scalar, int grid,
                     int *err, cudaStream_t s) {
 #define CALL(G, A, B, C) launch_tc<G, A, B, C>(p, grid, err, s)
+  HOLO_TC_DISPATCH(groups, poly16, scalar, CALL)
+#undef CALL
+}
+
+int launch_split_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items,
+                            int *queue, int groups, int poly16, bool scalar, int grid, int *err,
+                            cudaStream_t s) {
+#define CALL(G, A, B, C) launch_tc_batched<G, A, B, C>(probs, items, n_items, queue, grid, err, s)
   HOLO_TC_DISPATCH(groups, poly16, scalar, CALL)
 #undef CALL
 }
