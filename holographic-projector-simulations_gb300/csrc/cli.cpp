@@ -14,7 +14,8 @@
 //
 // Long options added here: --lambda, --precision fp64|split32, --mc SUB,
 // --seed S, --mc-block B, --amplitude-only (PROJECT_PHASE=0), --reference-distance,
-// --ref-compat, --out DIR (generated mode, default ../tmp/ as the reference), --device.
+// --ref-compat, --out DIR (generated mode, default ../tmp/ as the reference), --device,
+// --shape (the generated object's shape; the reference fixes it at compile time).
 //
 // Exit codes: 0 success; 2 bad arguments or files; 4 non-finite output (the
 // reference's check_complex exit, cuda/util.h:54-60); 3 a library error.
@@ -43,6 +44,9 @@ struct Range {
   T min, max;
 };
 
+// Shapes of the generated object (the reference's Shape, cuda/main.h:9).
+enum class Shape { Line, LogLine, Circle, DottedCircle };
+
 struct Params {
   size_t planes_obj = 1, planes_projection = 1;
   size_t n_obj = 1, n_projector = (size_t)kNSqrt * kNSqrt, n_projection = (size_t)kNSqrt * kNSqrt;
@@ -65,6 +69,7 @@ struct Params {
   uint64_t seed = 0;
   int mc_block = 256;
   bool amplitude_only = false;
+  Shape shape = Shape::Circle;  // the reference's generated object (cuda/main.cu:55)
   double reference_distance = 0.25;  // DISTANCE_REFERENCE_WAVE (cuda/macros.h:26-28)
   bool ref_compat = false;
   std::string out_dir = "../tmp/";
@@ -108,12 +113,14 @@ void show_help(const char *p) {
       "\t--ref-compat          \tReproduce the reference's -F (z from x at u onto v)\n"
       "\t--out DIR             \tOutput directory of the generated mode (default ../tmp/)\n"
       "\t--device D            \tCUDA device\n"
+      "\t--shape S             \tGenerated object: circle (default), dotted-circle, line, log-line\n"
       "\n",
       p);
 }
 
 bool parse(int argc, char **argv, Params *p, int *exit_code) {
-  enum { O_LAMBDA = 1000, O_PREC, O_MC, O_SEED, O_MCB, O_AMP, O_REFD, O_COMPAT, O_OUT, O_DEV };
+  enum { O_LAMBDA = 1000, O_PREC, O_MC, O_SEED, O_MCB, O_AMP, O_REFD, O_COMPAT, O_OUT, O_DEV,
+         O_SHAPE };
   static struct option longopts[] = {{"lambda", required_argument, 0, O_LAMBDA},
                                      {"precision", required_argument, 0, O_PREC},
                                      {"mc", required_argument, 0, O_MC},
@@ -124,6 +131,7 @@ bool parse(int argc, char **argv, Params *p, int *exit_code) {
                                      {"ref-compat", no_argument, 0, O_COMPAT},
                                      {"out", required_argument, 0, O_OUT},
                                      {"device", required_argument, 0, O_DEV},
+                                     {"shape", required_argument, 0, O_SHAPE},
                                      {"help", no_argument, 0, 'h'},
                                      {0, 0, 0, 0}};
   int ch;
@@ -173,6 +181,13 @@ bool parse(int argc, char **argv, Params *p, int *exit_code) {
       case O_COMPAT: p->ref_compat = true; break;
       case O_OUT: p->out_dir = std::string(optarg) + "/"; break;
       case O_DEV: p->device = strtol(optarg, 0, 10); break;
+      case O_SHAPE:
+        if (!strcmp(optarg, "circle")) p->shape = Shape::Circle;
+        else if (!strcmp(optarg, "dotted-circle")) p->shape = Shape::DottedCircle;
+        else if (!strcmp(optarg, "line")) p->shape = Shape::Line;
+        else if (!strcmp(optarg, "log-line")) p->shape = Shape::LogLine;
+        else { fprintf(stderr, "unknown shape %s\n", optarg); *exit_code = 2; return false; }
+        break;
       case 'h':
       default:
         show_help(argv[0]);
@@ -272,8 +287,14 @@ bool lattice(std::vector<double> &v, const holo_io::Plane &p) {
   return true;
 }
 
-// init::sparse_plane with Shape::Circle (cuda/init.h:160-234)
-void circle(std::vector<double> &u, double width, const double *offset, double modulate) {
+// init::sparse_plane (cuda/init.h:160-234) for the reference's Shape (cuda/main.h:9):
+// the object's points on a line, a line with geometric spacing, a circle, or a
+// circle around a centre point.  Like the reference, line shapes set x only and the
+// dotted circle leaves point 0 as it was (so y, and that point, keep the values of
+// the previous object plane), then the x/y offset is added to every point.
+
+void object_points(std::vector<double> &u, Shape shape, double width, const double *offset,
+                   double modulate) {
   const size_t n = u.size() / 3;
   for (size_t i = 0; i < n; ++i) u[3 * i + 2] = offset[2];
   if (n == 1) {
@@ -281,11 +302,35 @@ void circle(std::vector<double> &u, double width, const double *offset, double m
     u[1] = offset[1];
     return;
   }
-  const double radius = width / 2.0, d_phase = kTwoPi / (double)n,
-               arbitrary_offset = 0.1125 + modulate * kTwoPi;
-  for (size_t i = 0; i < n; ++i) {
-    u[3 * i] = sin(i * d_phase + arbitrary_offset) * radius;
-    u[3 * i + 1] = cos(i * d_phase + arbitrary_offset) * radius;
+  const double radius = width / 2.0, arbitrary_offset = 0.1125 + modulate * kTwoPi;
+  switch (shape) {
+    case Shape::Line: {
+      const double du = width / (double)(n - 1), half_width = width / 2.0;
+      for (size_t i = 0; i < n; ++i) u[3 * i] = i * du - half_width;
+      break;
+    }
+    case Shape::LogLine: {
+      // geomspace(n, 1, 1 + width) (cuda/algebra.h:55-91): 10^(linspace of the logs)
+      const double a = log10(1.0), b = log10(1.0 + width), delta = (b - a) / (n - 1.0);
+      for (size_t i = 0; i < n; ++i) u[3 * i] = pow(10.0, a + delta * i) - 1 + width / 2.;
+      break;
+    }
+    case Shape::Circle: {
+      const double d_phase = kTwoPi / (double)n;
+      for (size_t i = 0; i < n; ++i) {
+        u[3 * i] = sin(i * d_phase + arbitrary_offset) * radius;
+        u[3 * i + 1] = cos(i * d_phase + arbitrary_offset) * radius;
+      }
+      break;
+    }
+    case Shape::DottedCircle: {
+      const double d_phase = kTwoPi / (double)(n - 1);
+      for (size_t i = 1; i < n; ++i) {
+        u[3 * i] = sin(i * d_phase + arbitrary_offset) * radius;
+        u[3 * i + 1] = cos(i * d_phase + arbitrary_offset) * radius;
+      }
+      break;
+    }
   }
   if (offset[0] != 0 || offset[1] != 0)
     for (size_t i = 0; i < n; ++i) {
@@ -495,7 +540,7 @@ int generated_mode(Runner &R, const Params &p) {
     const double obj_off[3] = {lerp(p.off_x, ratio), lerp(p.off_y, ratio), gerp(p.off_z, ratio)};
     holo_io::Plane x_plane{lerp(p.obj_width, ratio), {obj_off[0], obj_off[1], obj_off[2]}, 1.0,
                            false};
-    circle(u, x_plane.width, obj_off, i / (double)p.planes_obj);
+    object_points(u, p.shape, x_plane.width, obj_off, i / (double)p.planes_obj);
     holo_io::Plane y_plane{lerp(p.projector_width, ratio), {0, 0, 0}, p.aspect_projector,
                            p.randomize};
     if (!lattice(v, y_plane)) return lib_fail("cuRAND", -2);

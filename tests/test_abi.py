@@ -75,6 +75,8 @@ def test_cli_help_and_argument_errors(holo):
     assert r.returncode == 2
     r = subprocess.run([exe, "-w", "0"], capture_output=True, text=True)
     assert r.returncode == 2
+    r = subprocess.run([exe, "--shape", "square"], capture_output=True, text=True)
+    assert r.returncode == 2 and "shape" in r.stderr
 
 
 def test_library_has_no_cpu_fallback(holo, tmp_path):

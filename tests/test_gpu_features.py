@@ -293,6 +293,34 @@ def test_batched_mixed_geometry_groups(holo, orc):
         assert rel_l2(yb[idx], orc.transform_subset(amp, phase, u, v, idx, -1, LAM)) < 1e-5
 
 
+@pytest.mark.parametrize("shape", ["line", "log-line", "dotted-circle"])
+def test_cli_generated_object_shapes(holo, tmp_path, shape):
+    """--shape selects the reference's other object shapes (cuda/init.h:175-222): 16 points
+    of the default 1 mm wide object 0.35 m above the projector."""
+    r = subprocess.run([_cli(holo), "-x", "16", "-y", "1024", "-z", "256", "--shape", shape,
+                        "--out", str(tmp_path), "--precision", "split32"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    u = holo.io.read_dat(str(tmp_path / "u0.dat")).reshape(-1, 3)
+    n, width = 16, 1e-3
+    i = np.arange(n)
+    assert np.allclose(u[:, 2], 0.35)
+    if shape == "line":
+        assert np.allclose(u[:, 0], i * width / (n - 1) - width / 2, rtol=0, atol=1e-15)
+        assert np.all(u[:, 1] == 0.0)
+    elif shape == "log-line":
+        x = 10.0 ** np.linspace(0.0, np.log10(1.0 + width), n) - 1 + width / 2
+        assert np.allclose(u[:, 0], x, rtol=0, atol=1e-15)
+        assert np.all(u[:, 1] == 0.0)
+    else:
+        ang = i[1:] * 2 * np.pi / (n - 1) + 0.1125
+        assert np.all(u[0, :2] == 0.0)  # the centre point
+        assert np.allclose(u[1:, 0], np.sin(ang) * width / 2, rtol=0, atol=1e-15)
+        assert np.allclose(u[1:, 1], np.cos(ang) * width / 2, rtol=0, atol=1e-15)
+    ya = holo.io.read_dat(str(tmp_path / "y0_amp.dat"))
+    assert ya.size == 1024 and ya.max() == pytest.approx(1.0)
+
+
 def test_cli_rejects_bad_files(holo, tmp_path):
     holo.io.write_inputs(str(tmp_path), [1.0, 2.0], [0.0], [0, 0, 1, 0, 0, 1], [0, 0, 0])
     r = subprocess.run([_cli(holo), "-f", str(tmp_path)], capture_output=True, text=True)
