@@ -22,7 +22,11 @@
 // a' e^{i theta'} on packed f32x2 pairs (SC: the MUFU pairs in scalar FP32).
 // One more warp allocates the tensor memory and issues the MMAs (one thread),
 // tracked by mbarriers: full[b] (tcgen05.commit) and free[b] (16 consumer
-// arrivals).  Per pair on the CUDA cores: 3 FP32-pipe ops + 2 MUFU ops.
+// arrivals).  A last warp builds the next tile pair's FP64 frame while the
+// pairs of this one are summed: FP64 is slow on this part (a frame is ~6000
+// cycles of dependent FP64 work), so a frame built in the MMA warp held back
+// the first MMA of every tile.  Per pair on the CUDA cores: 3 FP32-pipe ops +
+// 2 MUFU ops.
 //
 // Tiles: 512 targets per CTA (4 blocks of 128), 1024 sources per tile (4 blocks
 // of 256); one CTA per SM (~200 KB of shared memory).  Every wait is bounded:
@@ -51,7 +55,7 @@ struct TcShape {
   static constexpr int NB = CG == 4 ? 256 : 192;
   static constexpr int CS = 4 * NB;
   static constexpr int Consumers = 4 * CG;        // consumer warps
-  static constexpr int Threads = 32 * (Consumers + 1);
+  static constexpr int Threads = 32 * (Consumers + 2);  // + the MMA warp + the frame warp
   static constexpr int Cols = NB / CG;            // columns per consumer warp per block
   static constexpr int Chunks = Cols / 16;        // 16-column loads per block
 };
@@ -155,7 +159,9 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
   uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(smem + L::misc);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + L::misc + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool producer = warp == kTcConsumers;
+  const bool consumer = warp < kTcConsumers;
+  const bool producer = warp == kTcConsumers;     // TMEM owner, MMA issue
+  const bool framer = warp == kTcConsumers + 1;   // next tile pair's frame
   constexpr int NC = kTcConsumers * 32;  // consumer threads
 
   if (tid == 0) {
@@ -220,16 +226,16 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
 
     for (int j = sb; j < se; ++j) {
       Frame *fr = frames + (j & 1);
-      // the first tile's frame here; the next ones by the MMA warp during the
+      // the first tile's frame here; the next ones by the frame warp during the
       // previous tile's pair work
-      if (tid == 0 && j == sb)
+      if (framer && lane == 0 && j == sb)
         build_frame(fr, P.tiles_t + 6 * (size_t)tt, P.tiles_s + 6 * (size_t)j, sk);
       tc_wait(bar_tma, par_tma, abort_flag, err);
       par_tma ^= 1u;
       __syncthreads();  // frame and staged records visible
 
       // ---- operands of this tile pair (consumer threads) ----
-      if (!producer && !*abort_flag) {
+      if (consumer && !*abort_flag) {
         const float f1x = fr->e1[0], f1y = fr->e1[1], f1z = fr->e1[2];
         const float f2x = fr->e2[0], f2y = fr->e2[1], f2z = fr->e2[2];
         const float fex = fr->ef[0], fey = fr->ef[1], fez = fr->ef[2];
@@ -302,11 +308,14 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
       ptx::tc_fence_after();
       if (tid == 0 && j + 1 < se && !*abort_flag) issue(j + 1);
 
-      if (producer) {
-        // ---- MMA issue: 4 target blocks x 4 source blocks, double-buffered ----
-        if (lane == 1 && j + 1 < se)
+      if (framer) {
+        // frames[(j + 1) & 1] was last read by the operand build of tile j - 1
+        if (lane == 0 && j + 1 < se)
           build_frame(frames + ((j + 1) & 1), P.tiles_t + 6 * (size_t)tt,
                       P.tiles_s + 6 * (size_t)(j + 1), sk);
+        __syncwarp();
+      } else if (producer) {
+        // ---- MMA issue: 4 target blocks x 4 source blocks, double-buffered ----
         if (lane == 0) {
           for (int blk = 0; blk < 16; ++blk) {
             const int m = blk >> 2, n = blk & 3, b = blk & 1;
