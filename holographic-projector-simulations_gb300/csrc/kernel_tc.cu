@@ -81,10 +81,11 @@ struct TcSmem {
   static constexpr size_t opa_one = opa_lo + kTcTT * kTcK * 4;         // float [128*8]: (1,1,1,0..)
   static constexpr size_t amp = opa_one + kTcM * kTcK * 4;             // float [CS]
   static constexpr size_t part = amp + kTcCS * 4;                      // float2 [CG][TT]
-  static constexpr size_t acc = part + CG * kTcTT * 8;                 // double2 [TT]
+  static constexpr size_t acc = part + CG * kTcTT * 8;                 // float4 [TT]
   static constexpr size_t tph = acc + kTcTT * 16;                      // float [TT]
   static constexpr size_t tsc = tph + kTcTT * 4;                       // float [TT]
-  static constexpr size_t frame = tsc + kTcTT * 4;                     // Frame [2]
+  static constexpr size_t tgeo = tsc + kTcTT * 4;                      // float [6][TT]
+  static constexpr size_t frame = tgeo + 6 * kTcTT * 4;                // Frame [2]
   static constexpr size_t bars = (frame + 2 * sizeof(Frame) + 15) / 16 * 16;  // uint64 [5]
   static constexpr size_t misc = bars + 5 * 8;                         // uint32 taddr, abort
   static constexpr size_t bytes = misc + 16;
@@ -150,9 +151,12 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
   float *opa_one = reinterpret_cast<float *>(smem + L::opa_one);
   float *amp = reinterpret_cast<float *>(smem + L::amp);
   float2 *part = reinterpret_cast<float2 *>(smem + L::part);
-  double2 *acc = reinterpret_cast<double2 *>(smem + L::acc);
+  // per target, the running sum of the tile sums as float-float pairs
+  // (re hi, re lo, im hi, im lo): FP64 runs at a small fraction of the FP32 rate here
+  float4 *acc = reinterpret_cast<float4 *>(smem + L::acc);
   float *tph = reinterpret_cast<float *>(smem + L::tph);
   float *tsc = reinterpret_cast<float *>(smem + L::tsc);
+  float *tgeo = reinterpret_cast<float *>(smem + L::tgeo);  // this item's target records
   Frame *frames = reinterpret_cast<Frame *>(smem + L::frame);  // tile j in frames[j & 1]
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bars);
   uint64_t *bar_tma = bars, *full = bars + 1, *freeb = bars + 3;
@@ -221,7 +225,12 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
       ptx::bulk_g2s(raw_geo, P.geo_s + (size_t)j * kTcCS * 6, kTcCS * 6 * sizeof(float), bar_tma);
       ptx::bulk_g2s(raw_apf, P.apf_s + (size_t)j * kTcCS, kTcCS * sizeof(float2), bar_tma);
     };
-    for (int t = tid; t < kTcTT; t += kTcThreads) acc[t] = make_double2(0.0, 0.0);
+    for (int t = tid; t < kTcTT; t += kTcThreads) {
+      acc[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+      const int ti = tt * kTcTT + t;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) tgeo[k * kTcTT + t] = ti < P.M ? P.geo_t[6 * (size_t)ti + k] : 0.f;
+    }
     if (tid == 0 && sb < se && !*abort_flag) issue(sb);
 
     for (int j = sb; j < se; ++j) {
@@ -246,9 +255,18 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
           ah[d] = fr->ah[d];
           al[d] = fr->al[d];
         }
-        for (int i = tid; i < kTcCS; i += NC) {
-          float g[kTcK] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-          float a3[3] = {0.f, 0.f, 0.f}, am = 0.f;
+        // the source rows of this thread: all computed, then all stored, so that
+        // their dependent chains interleave
+        constexpr int R = kTcCS / NC;
+        static_assert(kTcCS % NC == 0, "source rows per consumer thread");
+        float g[R][kTcK], a3[R][3], am[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int i = tid + r * NC;
+#pragma unroll
+          for (int k = 0; k < kTcK; ++k) g[r][k] = 0.f;
+          a3[r][0] = a3[r][1] = a3[r][2] = 0.f;
+          am[r] = 0.f;
           if (j * kTcCS + i < P.N) {
             const float *q = raw_geo + 6 * i;
             const float sh[3] = {q[0], q[1], q[2]}, sl[3] = {q[3], q[4], q[5]};
@@ -261,31 +279,31 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
             const float Sy = fmaf(f2x, sh[0], fmaf(f2y, sh[1], f2z * sh[2]));
             const float Ps = fmaf(fex, sh[0], fmaf(fey, sh[1], fez * sh[2]));
             const float s2 = fmaf(Sx, Sx, Sy * Sy);
-            g[0] = s2; g[1] = Sx; g[2] = Sy; g[3] = Ps;
-            g[4] = Ps * s2; g[5] = Ps * Sx; g[6] = Ps * Sy;
+            g[r][0] = s2; g[r][1] = Sx; g[r][2] = Sy; g[r][3] = Ps;
+            g[r][4] = Ps * s2; g[r][5] = Ps * Sx; g[r][6] = Ps * Sy;
             // sign A = a0 + a1 + a2 exactly, each part a TF32 number
-            a3[0] = ptx::to_tf32(sA);
-            const float r1 = __fsub_rn(sA, a3[0]);
-            a3[1] = ptx::to_tf32(r1);
-            a3[2] = ptx::to_tf32(__fsub_rn(r1, a3[1]));
-            am = pa.y * fmaf(Ps, ir0, 1.f);
+            a3[r][0] = ptx::to_tf32(sA);
+            const float r1 = __fsub_rn(sA, a3[r][0]);
+            a3[r][1] = ptx::to_tf32(r1);
+            a3[r][2] = ptx::to_tf32(__fsub_rn(r1, a3[r][1]));
+            am[r] = pa.y * fmaf(Ps, ir0, 1.f);
           }
-          store_row_split(opb_hi, opb_lo, i, g);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int i = tid + r * NC;
+          store_row_split(opb_hi, opb_lo, i, g[r]);
           const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-          *reinterpret_cast<float4 *>(opb_a + tc_off(i, 0)) = make_float4(a3[0], a3[1], a3[2], 0.f);
+          *reinterpret_cast<float4 *>(opb_a + tc_off(i, 0)) =
+              make_float4(a3[r][0], a3[r][1], a3[r][2], 0.f);
           *reinterpret_cast<float4 *>(opb_a + tc_off(i, 4)) = z;
-          amp[i] = am;
+          amp[i] = am[r];
         }
         // targets: one per consumer thread (the first kTcTT of them)
         if (tid < kTcTT) {
           const int t = tid;
-          const int ti = tt * kTcTT + t;
-          float th[3] = {0.f, 0.f, 0.f}, tl[3] = {0.f, 0.f, 0.f};
-          if (ti < P.M) {
-            const float *q = P.geo_t + 6 * (size_t)ti;
-            th[0] = q[0]; th[1] = q[1]; th[2] = q[2];
-            tl[0] = q[3]; tl[1] = q[4]; tl[2] = q[5];
-          }
+          const float th[3] = {tgeo[t], tgeo[kTcTT + t], tgeo[2 * kTcTT + t]};
+          const float tl[3] = {tgeo[3 * kTcTT + t], tgeo[4 * kTcTT + t], tgeo[5 * kTcTT + t]};
           float S, E, S2, E2;
           dot3_ff(ah, al, th, tl, S, E);
           two_sum(S, fr->b0h, S2, E2);
@@ -415,7 +433,7 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
       }
       __syncthreads();  // partial sums complete
 
-      // ---- per target: sum the column groups, scale, rotate, carry in FP64 ----
+      // ---- per target: sum the column groups, scale, rotate, carry (float-float) ----
       if (tid < kTcTT) {
         const int t = tid;
         float sx = 0.f, sy = 0.f;
@@ -430,9 +448,14 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
         const float im = sgn * sy * sc;
         float sr, cr;
         __sincosf(tph[t], &sr, &cr);
-        double2 a = acc[t];
-        a.x += (double)fmaf(re, cr, -im * sr);
-        a.y += (double)fmaf(re, sr, im * cr);
+        float4 a = acc[t];
+        float h, e;
+        two_sum(a.x, fmaf(re, cr, -im * sr), h, e);  // h + e: the exact sum
+        a.x = h;
+        a.y = __fadd_rn(a.y, e);
+        two_sum(a.z, fmaf(re, sr, im * cr), h, e);
+        a.z = h;
+        a.w = __fadd_rn(a.w, e);
         acc[t] = a;
       }
       __syncthreads();  // operands, partials and per-target data are rewritten next tile
@@ -441,7 +464,8 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
     for (int t = tid; t < kTcTT; t += kTcThreads) {
       const int ti = tt * kTcTT + t;
       if (ti < P.M) {
-        const double2 v = acc[t];
+        const float4 a = acc[t];
+        const double2 v = make_double2((double)a.x + (double)a.y, (double)a.z + (double)a.w);
         if (P.splits == 1)
           P.y[P.order_t[ti]] = v;
         else
