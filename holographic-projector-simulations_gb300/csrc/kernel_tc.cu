@@ -110,8 +110,8 @@ __device__ __forceinline__ void store_row_split(float *hi, float *lo, int r, con
   float h[kTcK], l[kTcK];
 #pragma unroll
   for (int k = 0; k < kTcK; ++k) {
-    h[k] = ptx::to_tf32(x[k]);
-    l[k] = ptx::to_tf32(__fsub_rn(x[k], h[k]));
+    h[k] = ptx::to_tf32_int(x[k]);
+    l[k] = ptx::to_tf32_int(__fsub_rn(x[k], h[k]));
   }
   *reinterpret_cast<float4 *>(hi + tc_off(r, 0)) = make_float4(h[0], h[1], h[2], h[3]);
   *reinterpret_cast<float4 *>(hi + tc_off(r, 4)) = make_float4(h[4], h[5], h[6], h[7]);
@@ -282,10 +282,10 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
             g[r][0] = s2; g[r][1] = Sx; g[r][2] = Sy; g[r][3] = Ps;
             g[r][4] = Ps * s2; g[r][5] = Ps * Sx; g[r][6] = Ps * Sy;
             // sign A = a0 + a1 + a2 exactly, each part a TF32 number
-            a3[r][0] = ptx::to_tf32(sA);
+            a3[r][0] = ptx::to_tf32_int(sA);
             const float r1 = __fsub_rn(sA, a3[r][0]);
-            a3[r][1] = ptx::to_tf32(r1);
-            a3[r][2] = ptx::to_tf32(__fsub_rn(r1, a3[r][1]));
+            a3[r][1] = ptx::to_tf32_int(r1);
+            a3[r][2] = ptx::to_tf32_int(__fsub_rn(r1, a3[r][1]));
             am[r] = pa.y * fmaf(Ps, ir0, 1.f);
           }
         }

@@ -168,6 +168,15 @@ __device__ __forceinline__ float to_tf32(float x) {
   return __uint_as_float(r);
 }
 
+// The same rounding (to nearest, ties away from zero, onto the 10-bit TF32
+// mantissa) by integer arithmetic on the bit pattern, for finite x: adding half a
+// TF32 ulp to the magnitude bits and clearing the 13 dropped bits carries into
+// the exponent where it must.  Two integer-pipe instructions instead of one
+// conversion, for code that converts many operands at once.
+__device__ __forceinline__ float to_tf32_int(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xffffe000u);
+}
+
 // MUFU approximations (PTX .approx instructions, flush-to-zero).
 // ---- packed FP32 pairs (sm_100+ f32x2 arithmetic: one instruction, two lanes of
 // work).  A pair lives in one 64-bit register: low half first.
