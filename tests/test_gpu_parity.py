@@ -76,6 +76,25 @@ def test_ragged_sizes(holo, orc, prec, n, m):
         assert rel_l2(y, orc.transform(amp, phase, u, v, sign, LAM)) < TOL[prec]
 
 
+@pytest.mark.parametrize("n,m", [(1000, 777), (1025, 2049), (3, 600), (5000, 1)])
+def test_tensor_core_variants_ragged(holo, orc, n, m):
+    """Every tensor-core build on sizes that fill neither the 1024- (768-) source tiles nor
+    the 512-target tiles: the padding sources, the targets past M in the last tile and the
+    per-item staging of target records must all drop out."""
+    rng = np.random.default_rng(n + 7 * m)
+    u = grid(int(np.ceil(np.sqrt(n))), 10e-6, 0.35)[:n]
+    v = grid(int(np.ceil(np.sqrt(m))), 7.56e-6, 0.0)[:m]
+    amp, phase = rng.uniform(0, 1, n), rng.uniform(0, 2 * np.pi, n)
+    refs = {s: orc.transform(amp, phase, u, v, s, LAM) for s in (-1, 1)}
+    tc = [var for var in holo.variants("split32") if var["pair_loop"] == 3]
+    assert tc, "no tensor-core build in the variant table"
+    for var in tc:
+        for s in (-1, 1):
+            y = holo.transform(amp, phase, u, v, s, LAM, precision="split32",
+                               variant=var["variant"])
+            assert rel_l2(y, refs[s]) < TOL["split32"], (var, s)
+
+
 @pytest.mark.parametrize("prec", ["fp64", "split32"])
 def test_tilted_and_3d_geometry(holo, orc, prec):
     """Non-parallel planes and a 3-D cloud (the frame basis is built per tile pair)."""
