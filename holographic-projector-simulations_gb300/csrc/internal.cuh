@@ -193,14 +193,15 @@ int launch_gather_apf(const double *amp, const double *phase, const int32_t *ord
                       int n_pad, float2 *out, cudaStream_t s);
 
 // kernel_split.cu
-// kernel_tc.cu: the tensor-core split kernel (pair model 3) with `groups` (4 or 6)
-// consumer warps per TMEM lane group (source tiles of 1024 or 768), `poly16` of every
-// 16 source pairs on the FMA-pipe sin/cos, `scalar`: MUFU pairs accumulated unpacked
-int launch_split_tc(const SplitProblem &p, int groups, int poly16, bool scalar, int grid,
-                    int *err, cudaStream_t s);
-int split_tc_occupancy(int groups, int poly16, bool scalar, int *ctas_per_sm);
+// kernel_tc.cu: the tensor-core split kernel (pair model 3) on source tiles of `cs`
+// (1024, 512 or 256: 4 consumer warps per TMEM lane group and MMA blocks of 256
+// sources; 768: 6 consumer warps, blocks of 192), `poly16` of every 16 source pairs
+// on the FMA-pipe sin/cos, `scalar`: MUFU pairs accumulated unpacked
+int launch_split_tc(const SplitProblem &p, int cs, int poly16, bool scalar, int grid, int *err,
+                    cudaStream_t s);
+int split_tc_occupancy(int cs, int poly16, bool scalar, int *ctas_per_sm);
 int launch_split_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items,
-                            int *queue, int groups, int poly16, bool scalar, int grid, int *err,
+                            int *queue, int cs, int poly16, bool scalar, int grid, int *err,
                             cudaStream_t s);
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
                  int *err, cudaStream_t s);

@@ -514,6 +514,11 @@ constexpr Variant kVariants[] = {
     {512, 1, 768, 6, 3, 1, 0, 1},      // 41
     {512, 1, 768, 5, 3, 1, 0, 1},      // 42
     {512, 1, 768, 7, 3, 1, 0, 1},      // 43
+    // pair model 3 on shorter source tiles (512, 256): four times and twice the tile
+    // pairs of variant 34, for point sets whose error bound needs narrower tiles
+    {512, 1, 512, 6, 3, 1, 0, 1},      // 44
+    {512, 1, 256, 6, 3, 1, 0, 1},      // 45
+    {128, 4, 256, 1, 2, 1},            // 46: packed model 2, TT 512 x source tiles of 256
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -563,18 +568,25 @@ int split_variant_count() { return kNumVariants; }
 Variant split_variant(int i) { return kVariants[i]; }
 
 // The tensor-core variants have no Monte Carlo or constant-phase build: those
-// calls run a CUDA-core variant with the same tiles (512 targets and 1024 or 768
-// sources: variant 26 or 40).
+// calls run a CUDA-core variant with the same tiles (512 targets and 1024, 768, 512
+// or 256 sources: variant 26, 40, 29 or 46).
 static bool is_tc(int v) { return v >= 0 && v < kNumVariants && kVariants[v].tc; }
-static int tc_fallback(int v) { return kVariants[v].cs == 768 ? 40 : 26; }
-static int tc_groups(int v) { return kVariants[v].cs == 768 ? 6 : 4; }
+static int tc_fallback(int v) {
+  switch (kVariants[v].cs) {
+    case 768: return 40;
+    case 512: return 29;
+    case 256: return 46;
+    default: return 26;
+  }
+}
 
 std::vector<int> split_preferences(size_t N, size_t M) {
   (void)N;
   if (M < 1024) return {3, 4};
-  // fastest first: the tensor-core phase (pair model 3), then the CUDA-core pair
-  // models 2, 1, 0 on ever smaller tiles
-  return {34, 23, 13, 9, 27, 21, 16, 11, 3, 4};
+  // fastest first: the tensor-core phase (pair model 3) on source tiles of 1024,
+  // 512 and 256 (measured on the config-2 y pass: 2.87, 2.66, 2.38e12 pairs/s), then
+  // the CUDA-core pair models 2, 1, 0 on ever smaller tiles
+  return {34, 44, 45, 23, 13, 9, 27, 21, 16, 11, 3, 4};
 }
 
 #define HOLO_SPLIT_DISPATCH(V, CALL)                      \
@@ -610,6 +622,7 @@ std::vector<int> split_preferences(size_t N, size_t M) {
     case 28: return CALL(256, 4, 512, 0 | 96);            \
     case 29: return CALL(128, 4, 512, 1 | 96);            \
     case 40: return CALL(128, 4, 768, 1 | 96);            \
+    case 46: return CALL(128, 4, 256, 1 | 96);            \
     case 30: return CALL(512, 4, 1024, 1 | 96);           \
     case 31: return CALL(512, 4, 1024, 0 | 96 | 128);     \
     case 32: return CALL(512, 2, 1024, 0 | 96 | 128);     \
@@ -620,7 +633,7 @@ int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase,
                  int *err, cudaStream_t s) {
   if (is_tc(variant)) {
     if (!const_phase && !mc)
-      return launch_split_tc(p, tc_groups(variant), kVariants[variant].poly,
+      return launch_split_tc(p, kVariants[variant].cs, kVariants[variant].poly,
                              kVariants[variant].sc != 0, grid, err, s);
     variant = tc_fallback(variant);
   }
@@ -632,7 +645,7 @@ int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase,
 int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, int n_items,
                          int *queue, int variant, int grid, int *err, cudaStream_t s) {
   if (is_tc(variant))
-    return launch_split_tc_batched(probs_dev, items, n_items, queue, tc_groups(variant),
+    return launch_split_tc_batched(probs_dev, items, n_items, queue, kVariants[variant].cs,
                                    kVariants[variant].poly, kVariants[variant].sc != 0, grid, err,
                                    s);
 #define CALL(T, R, C, P) batched_variant<T, R, C, P>(probs_dev, items, n_items, queue, grid, err, s)
@@ -643,7 +656,7 @@ int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, i
 int split_occupancy(int variant, bool mc, int *ctas_per_sm) {
   if (is_tc(variant)) {
     if (!mc)
-      return split_tc_occupancy(tc_groups(variant), kVariants[variant].poly,
+      return split_tc_occupancy(kVariants[variant].cs, kVariants[variant].poly,
                                 kVariants[variant].sc != 0, ctas_per_sm);
     variant = tc_fallback(variant);
   }

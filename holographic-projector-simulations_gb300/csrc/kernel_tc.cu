@@ -28,8 +28,11 @@
 // the first MMA of every tile.  Per pair on the CUDA cores: 3 FP32-pipe ops +
 // 2 MUFU ops.
 //
-// Tiles: 512 targets per CTA (4 blocks of 128), 1024 sources per tile (4 blocks
-// of 256); one CTA per SM (~200 KB of shared memory).  Every wait is bounded:
+// Tiles: 512 targets per CTA (4 blocks of 128), NBLK blocks of 256 sources per
+// tile (1024, 512 or 256 sources; 768 in blocks of 192 with 24 consumer warps);
+// one CTA per SM (up to 213 KB of shared memory).  Shorter source tiles narrow
+// the tile pairs, which tightens the error bound of the first-order model for
+// close or wide point sets, at more per-tile work per pair.  Every wait is bounded:
 // after a timeout the kernel raises the device error word and skips the rest
 // of its work, then waits (bounded) for the MMAs it issued and frees the
 // tensor memory.
@@ -47,13 +50,14 @@ constexpr int kTcCols = 512;                  // TMEM columns allocated: two acc
 constexpr uint32_t kTcLbo = 128, kTcSbo = 256;  // operand layout (bytes), see tc_off
 
 // Shape of one build: CG column groups of consumer warps per TMEM lane group (4 lane
-// groups of 32 targets), NB sources per MMA block (TMEM columns per buffer), CS = 4 NB
+// groups of 32 targets), NB sources per MMA block (TMEM columns per buffer), CS = NBLK NB
 // sources per tile.  CG = 4: 16 consumer warps, NB 256; CG = 6: 24 warps, NB 192.
-template <int CG>
+template <int CG, int NBLK>
 struct TcShape {
   static_assert(CG == 4 || CG == 6, "tensor-core split kernel: 4 or 6 column groups");
+  static_assert(NBLK == 1 || NBLK == 2 || NBLK == 4, "tensor-core split kernel: 1, 2 or 4 blocks");
   static constexpr int NB = CG == 4 ? 256 : 192;
-  static constexpr int CS = 4 * NB;
+  static constexpr int CS = NBLK * NB;
   static constexpr int Consumers = 4 * CG;        // consumer warps
   static constexpr int Threads = 32 * (Consumers + 2);  // + the MMA warp + the frame warp
   static constexpr int Cols = NB / CG;            // columns per consumer warp per block
@@ -68,9 +72,9 @@ __host__ __device__ __forceinline__ int tc_off(int r, int k) {
   return (r >> 3) * 64 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3);
 }
 
-template <int CG>
+template <int CG, int NBLK>
 struct TcSmem {
-  static constexpr int kTcCS = TcShape<CG>::CS;
+  static constexpr int kTcCS = TcShape<CG, NBLK>::CS;
   static constexpr size_t raw_geo = 0;                                 // float [CS*6]
   static constexpr size_t raw_apf = raw_geo + kTcCS * 6 * 4;           // float2 [CS]
   static constexpr size_t opb_hi = raw_apf + kTcCS * 8;                // float [CS*8]
@@ -90,12 +94,16 @@ struct TcSmem {
   static constexpr size_t misc = bars + 5 * 8;                         // uint32 taddr, abort
   static constexpr size_t bytes = misc + 16;
 };
-static_assert(TcSmem<4>::bytes <= 227 * 1024 && TcSmem<6>::bytes <= 227 * 1024,
-              "tensor-core split kernel: shared memory");
-static_assert(TcSmem<4>::opb_hi % 128 == 0 && TcSmem<4>::opa_hi % 128 == 0 &&
-                  TcSmem<6>::opb_hi % 128 == 0 && TcSmem<6>::opa_hi % 128 == 0 &&
-                  TcSmem<6>::opa_one % 16 == 0 && TcSmem<6>::amp % 16 == 0,
-              "operand alignment");
+template <int CG, int NBLK>
+constexpr bool tc_layout_ok() {
+  using L = TcSmem<CG, NBLK>;
+  return L::bytes <= 227 * 1024 && L::raw_apf % 16 == 0 && L::opb_hi % 128 == 0 &&
+         L::opb_lo % 128 == 0 && L::opb_a % 128 == 0 && L::opa_hi % 128 == 0 &&
+         L::opa_lo % 128 == 0 && L::opa_one % 128 == 0 && L::amp % 16 == 0 && L::acc % 16 == 0;
+}
+static_assert(tc_layout_ok<4, 4>() && tc_layout_ok<4, 2>() && tc_layout_ok<4, 1>() &&
+                  tc_layout_ok<6, 4>(),
+              "tensor-core split kernel: shared memory size and operand alignment");
 
 __device__ __forceinline__ void split_range_tc(int n, int splits, int s, int *b, int *e) {
   *b = (int)(((long long)n * s) / splits);
@@ -132,13 +140,13 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
 // BATCHED: work items (problem, target tile, source range, split) come from a
 // device queue (atomic counter) and each names its own problem descriptor;
 // otherwise item i of problem P0 is target tile i / splits, split i % splits.
-template <int CG, int NPP0, int NPP1, bool SC, bool BATCHED>
-__global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
+template <int CG, int NBLK, int NPP0, int NPP1, bool SC, bool BATCHED>
+__global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
     k_split_tc(const SplitProblem P0, const SplitProblem *__restrict__ probs,
                const WorkItem *__restrict__ items, int n_items, int *queue, int *err) {
   extern __shared__ __align__(128) unsigned char smem[];
-  using L = TcSmem<CG>;
-  using S = TcShape<CG>;
+  using L = TcSmem<CG, NBLK>;
+  using S = TcShape<CG, NBLK>;
   constexpr int kTcCS = S::CS, kTcN = S::NB, kTcConsumers = S::Consumers;
   constexpr int kTcThreads = S::Threads;
   float *raw_geo = reinterpret_cast<float *>(smem + L::raw_geo);
@@ -257,8 +265,8 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
         }
         // the source rows of this thread: all computed, then all stored, so that
         // their dependent chains interleave
-        constexpr int R = kTcCS / NC;
-        static_assert(kTcCS % NC == 0, "source rows per consumer thread");
+        constexpr int R = (kTcCS + NC - 1) / NC;
+        static_assert(kTcCS % NC == 0 || NC % kTcCS == 0, "source rows per consumer thread");
         float g[R][kTcK], a3[R][3], am[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -267,7 +275,7 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
           for (int k = 0; k < kTcK; ++k) g[r][k] = 0.f;
           a3[r][0] = a3[r][1] = a3[r][2] = 0.f;
           am[r] = 0.f;
-          if (j * kTcCS + i < P.N) {
+          if (i < kTcCS && j * kTcCS + i < P.N) {
             const float *q = raw_geo + 6 * i;
             const float sh[3] = {q[0], q[1], q[2]}, sl[3] = {q[3], q[4], q[5]};
             const float2 pa = raw_apf[i];
@@ -292,6 +300,7 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const int i = tid + r * NC;
+          if (i >= kTcCS) break;
           store_row_split(opb_hi, opb_lo, i, g[r]);
           const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
           *reinterpret_cast<float4 *>(opb_a + tc_off(i, 0)) =
@@ -333,10 +342,10 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
                       P.tiles_s + 6 * (size_t)(j + 1), sk);
         __syncwarp();
       } else if (producer) {
-        // ---- MMA issue: 4 target blocks x 4 source blocks, double-buffered ----
+        // ---- MMA issue: 4 target blocks x NBLK source blocks, double-buffered ----
         if (lane == 0) {
-          for (int blk = 0; blk < 16; ++blk) {
-            const int m = blk >> 2, n = blk & 3, b = blk & 1;
+          for (int blk = 0; blk < 4 * NBLK; ++blk) {
+            const int m = blk / NBLK, n = blk % NBLK, b = blk & 1;
             if (uses[b] > 0) tc_wait(&freeb[b], (uses[b] - 1) & 1u, abort_flag, err);
             if (*abort_flag) break;
             ptx::tc_fence_after();
@@ -362,8 +371,8 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
         for (int m = 0; m < 4; ++m) {
           uint64_t re2 = 0ull, im2 = 0ull;
           float res[2] = {0.f, 0.f}, ims[2] = {0.f, 0.f};  // SC: the MUFU pairs
-          for (int n = 0; n < 4; ++n) {
-            const int b = (m * 4 + n) & 1;
+          for (int n = 0; n < NBLK; ++n) {
+            const int b = (m * NBLK + n) & 1;
             const bool ok =
                 __all_sync(0xffffffffu, tc_wait(&full[b], uses[b] & 1u, abort_flag, err));
             ++uses[b];
@@ -485,79 +494,83 @@ __global__ void __launch_bounds__(TcShape<CG>::Threads, 1)
   if (producer) ptx::tmem_dealloc(tbase, kTcCols);
 }
 
-template <int CG, int NPP0, int NPP1, bool SC>
+template <int CG, int NBLK, int NPP0, int NPP1, bool SC>
 int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
-  auto kern = k_split_tc<CG, NPP0, NPP1, SC, false>;
-  constexpr int bytes = (int)TcSmem<CG>::bytes;
-  HOLO_TRY((kernel_setup<k_split_tc<CG, NPP0, NPP1, SC, false>>(TcShape<CG>::Threads, bytes,
-                                                                 nullptr)));
+  auto kern = k_split_tc<CG, NBLK, NPP0, NPP1, SC, false>;
+  constexpr int bytes = (int)TcSmem<CG, NBLK>::bytes;
+  constexpr int threads = TcShape<CG, NBLK>::Threads;
+  HOLO_TRY((kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, SC, false>>(threads, bytes, nullptr)));
   const int n_items = p.n_ttiles * p.splits;
   if (n_items <= 0) return HOLO_OK;
-  kern<<<grid, TcShape<CG>::Threads, bytes, s>>>(p, nullptr, nullptr, n_items, nullptr, err);
+  kern<<<grid, threads, bytes, s>>>(p, nullptr, nullptr, n_items, nullptr, err);
   note_launches(1);
   HOLO_CUDA(cudaGetLastError());
   return HOLO_OK;
 }
 
-template <int CG, int NPP0, int NPP1, bool SC>
+template <int CG, int NBLK, int NPP0, int NPP1, bool SC>
 int launch_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items, int *queue,
                       int grid, int *err, cudaStream_t s) {
-  auto kern = k_split_tc<CG, NPP0, NPP1, SC, true>;
-  constexpr int bytes = (int)TcSmem<CG>::bytes;
-  HOLO_TRY((kernel_setup<k_split_tc<CG, NPP0, NPP1, SC, true>>(TcShape<CG>::Threads, bytes,
-                                                                nullptr)));
-  kern<<<grid, TcShape<CG>::Threads, bytes, s>>>(SplitProblem{}, probs, items, n_items, queue,
-                                                 err);
+  auto kern = k_split_tc<CG, NBLK, NPP0, NPP1, SC, true>;
+  constexpr int bytes = (int)TcSmem<CG, NBLK>::bytes;
+  constexpr int threads = TcShape<CG, NBLK>::Threads;
+  HOLO_TRY((kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, SC, true>>(threads, bytes, nullptr)));
+  kern<<<grid, threads, bytes, s>>>(SplitProblem{}, probs, items, n_items, queue, err);
   note_launches(1);
   HOLO_CUDA(cudaGetLastError());
   return HOLO_OK;
 }
 
-template <int CG, int NPP0, int NPP1, bool SC>
+template <int CG, int NBLK, int NPP0, int NPP1, bool SC>
 int occupancy_tc(int *out) {
-  constexpr int bytes = (int)TcSmem<CG>::bytes;
-  return kernel_setup<k_split_tc<CG, NPP0, NPP1, SC, false>>(TcShape<CG>::Threads, bytes, out);
+  constexpr int bytes = (int)TcSmem<CG, NBLK>::bytes;
+  return kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, SC, false>>(TcShape<CG, NBLK>::Threads,
+                                                                   bytes, out);
 }
 
-// builds: column groups, polynomial pairs per 16 (even chunk + odd chunk), scalar
-// MUFU accumulation
-#define HOLO_TC_DISPATCH(CGS, NP16, SCAL, CALL)                                        \
-  switch ((CGS) * 100 + (NP16) * 2 + ((SCAL) ? 1 : 0)) {                               \
-    case 408: return CALL(4, 2, 2, false);                                             \
-    case 410: return CALL(4, 2, 3, false);                                             \
-    case 412: return CALL(4, 3, 3, false);                                             \
-    case 413: return CALL(4, 3, 3, true);                                              \
-    case 414: return CALL(4, 3, 4, false);                                             \
-    case 415: return CALL(4, 3, 4, true);                                              \
-    case 416: return CALL(4, 4, 4, false);                                             \
-    case 610: return CALL(6, 2, 3, false);                                             \
-    case 612: return CALL(6, 3, 3, false);                                             \
-    case 614: return CALL(6, 3, 4, false);                                             \
-    default:                                                                           \
-      return fail(HOLO_ERR_INVALID, "tensor-core split kernel: no build for %d groups, %d of 16", \
-                  CGS, NP16);                                                          \
+// builds: source tile, polynomial pairs per 16 (even chunk + odd chunk), scalar MUFU
+// accumulation
+#define HOLO_TC_DISPATCH(CS, NP16, SCAL, CALL)                                            \
+  switch ((CS) * 100 + (NP16) * 2 + ((SCAL) ? 1 : 0)) {                                   \
+    case 102408: return CALL(4, 4, 2, 2, false);                                          \
+    case 102410: return CALL(4, 4, 2, 3, false);                                          \
+    case 102412: return CALL(4, 4, 3, 3, false);                                          \
+    case 102413: return CALL(4, 4, 3, 3, true);                                           \
+    case 102414: return CALL(4, 4, 3, 4, false);                                          \
+    case 102415: return CALL(4, 4, 3, 4, true);                                           \
+    case 102416: return CALL(4, 4, 4, 4, false);                                          \
+    case 51212: return CALL(4, 2, 3, 3, false);                                           \
+    case 25612: return CALL(4, 1, 3, 3, false);                                           \
+    case 76810: return CALL(6, 4, 2, 3, false);                                           \
+    case 76812: return CALL(6, 4, 3, 3, false);                                           \
+    case 76814: return CALL(6, 4, 3, 4, false);                                           \
+    default:                                                                              \
+      return fail(HOLO_ERR_INVALID,                                                       \
+                  "tensor-core split kernel: no build for source tiles of %d, %d of 16", CS, \
+                  NP16);                                                                  \
   }
 
 }  // namespace
 
-int launch_split_tc(const SplitProblem &p, int groups, int poly16, bool scalar, int grid,
-                    int *err, cudaStream_t s) {
-#define CALL(G, A, B, C) launch_tc<G, A, B, C>(p, grid, err, s)
-  HOLO_TC_DISPATCH(groups, poly16, scalar, CALL)
+int launch_split_tc(const SplitProblem &p, int cs, int poly16, bool scalar, int grid, int *err,
+                    cudaStream_t s) {
+#define CALL(G, NB, A, B, C) launch_tc<G, NB, A, B, C>(p, grid, err, s)
+  HOLO_TC_DISPATCH(cs, poly16, scalar, CALL)
 #undef CALL
 }
 
 int launch_split_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items,
-                            int *queue, int groups, int poly16, bool scalar, int grid, int *err,
+                            int *queue, int cs, int poly16, bool scalar, int grid, int *err,
                             cudaStream_t s) {
-#define CALL(G, A, B, C) launch_tc_batched<G, A, B, C>(probs, items, n_items, queue, grid, err, s)
-  HOLO_TC_DISPATCH(groups, poly16, scalar, CALL)
+#define CALL(G, NB, A, B, C) \
+  launch_tc_batched<G, NB, A, B, C>(probs, items, n_items, queue, grid, err, s)
+  HOLO_TC_DISPATCH(cs, poly16, scalar, CALL)
 #undef CALL
 }
 
-int split_tc_occupancy(int groups, int poly16, bool scalar, int *ctas_per_sm) {
-#define CALL(G, A, B, C) occupancy_tc<G, A, B, C>(ctas_per_sm)
-  HOLO_TC_DISPATCH(groups, poly16, scalar, CALL)
+int split_tc_occupancy(int cs, int poly16, bool scalar, int *ctas_per_sm) {
+#define CALL(G, NB, A, B, C) occupancy_tc<G, NB, A, B, C>(ctas_per_sm)
+  HOLO_TC_DISPATCH(cs, poly16, scalar, CALL)
 #undef CALL
 }
 
