@@ -84,11 +84,15 @@ struct TcSmem {
   static constexpr size_t opa_lo = opa_hi + kTcTT * kTcK * 4;          // float [TT*8]
   static constexpr size_t opa_one = opa_lo + kTcTT * kTcK * 4;         // float [128*8]: (1,1,1,0..)
   static constexpr size_t amp = opa_one + kTcM * kTcK * 4;             // float [CS]
-  static constexpr size_t part = amp + kTcCS * 4;                      // float2 [CG][TT]
-  static constexpr size_t acc = part + CG * kTcTT * 8;                 // float4 [TT]
-  static constexpr size_t tph = acc + kTcTT * 16;                      // float [TT]
-  static constexpr size_t tsc = tph + kTcTT * 4;                       // float [TT]
-  static constexpr size_t tgeo = tsc + kTcTT * 4;                      // float [6][TT]
+  // partial sums, [PB][CG][TT] float2: a tile's are carried during the next tile, and
+  // with fewer than three source blocks per tile a consumer can write the next
+  // tile's before a slower one has carried them, so those builds keep two buffers
+  static constexpr int PB = NBLK >= 3 ? 1 : 2;
+  static constexpr size_t part = amp + kTcCS * 4;
+  static constexpr size_t acc = part + PB * CG * kTcTT * 8;            // float4 [TT]
+  static constexpr size_t tph = acc + kTcTT * 16;                      // float [2][TT]
+  static constexpr size_t tsc = tph + 2 * kTcTT * 4;                   // float [2][TT]
+  static constexpr size_t tgeo = tsc + 2 * kTcTT * 4;                  // float [6][TT]
   static constexpr size_t frame = tgeo + 6 * kTcTT * 4;                // Frame [2]
   static constexpr size_t bars = (frame + 2 * sizeof(Frame) + 15) / 16 * 16;  // uint64 [5]
   static constexpr size_t misc = bars + 5 * 8;                         // uint32 taddr, abort
@@ -233,6 +237,33 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
       ptx::bulk_g2s(raw_geo, P.geo_s + (size_t)j * kTcCS * 6, kTcCS * 6 * sizeof(float), bar_tma);
       ptx::bulk_g2s(raw_apf, P.apf_s + (size_t)j * kTcCS, kTcCS * sizeof(float2), bar_tma);
     };
+    // per target: sum the column groups of tile jj, scale, rotate, carry (float-float);
+    // run by consumer thread t during the next tile, after its operand build, so
+    // that it fills the wait for that tile's first MMA block
+    auto carry = [&](int jj) {
+      const int t = tid;
+      float sx = 0.f, sy = 0.f;
+#pragma unroll
+      for (int c = 0; c < CG; ++c) {
+        const float2 v = part[((jj & 1) % L::PB) * CG * kTcTT + c * kTcTT + t];
+        sx += v.x;
+        sy += v.y;
+      }
+      const float sc = tsc[(jj & 1) * kTcTT + t];
+      const float re = sx * sc;
+      const float im = sgn * sy * sc;
+      float sr, cr;
+      __sincosf(tph[(jj & 1) * kTcTT + t], &sr, &cr);
+      float4 a = acc[t];
+      float h, e;
+      two_sum(a.x, fmaf(re, cr, -im * sr), h, e);  // h + e: the exact sum
+      a.x = h;
+      a.y = __fadd_rn(a.y, e);
+      two_sum(a.z, fmaf(re, sr, im * cr), h, e);
+      a.z = h;
+      a.w = __fadd_rn(a.w, e);
+      acc[t] = a;
+    };
     for (int t = tid; t < kTcTT; t += kTcThreads) {
       acc[t] = make_float4(0.f, 0.f, 0.f, 0.f);
       const int ti = tt * kTcTT + t;
@@ -325,8 +356,8 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
           const float f[kTcK] = {Iq, -2.f * Iq * Tx, -2.f * Iq * Ty, Kq * T2,
                                  Kq, -2.f * Kq * Tx, -2.f * Kq * Ty, 0.f};
           store_row_split(opa_hi, opa_lo, t, f);
-          tph[t] = B + sgn * Iq * T2;  // the target's rotation, incl. the Iq T2 term
-          tsc[t] = Iq * iak;           // 1 / Qt
+          tph[(j & 1) * kTcTT + t] = B + sgn * Iq * T2;  // the rotation, incl. the Iq T2 term
+          tsc[(j & 1) * kTcTT + t] = Iq * iak;           // 1 / Qt
         }
       }
       ptx::fence_proxy_async_smem();
@@ -366,6 +397,12 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
         }
         __syncwarp();
       } else {
+        // the previous tile's carry while this tile's first MMAs run: its partial
+        // sums are complete (written before the operand sync).  With one buffer
+        // (NBLK >= 3) they are rewritten only after block NBLK - 1 >= 2 of this
+        // tile, whose MMA waits for every consumer to free block 0, i.e. to have
+        // passed this point; with fewer blocks the next tile writes the other buffer
+        if (j > sb && tid < kTcTT && !*abort_flag) carry(j - 1);
         // ---- consumers: sin/cos and accumulation of a' e^{i theta'} ----
         const int lg = warp & 3, cg = warp >> 2;
         for (int m = 0; m < 4; ++m) {
@@ -436,39 +473,14 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
           ptx::unpack2(re2, x, y);
           const float re = (x + y) + (res[0] + res[1]);
           ptx::unpack2(im2, x, y);
-          part[cg * kTcTT + m * kTcM + 32 * lg + lane] =
+          part[((j & 1) % L::PB) * CG * kTcTT + cg * kTcTT + m * kTcM + 32 * lg + lane] =
               make_float2(re, (x + y) + (ims[0] + ims[1]));
         }
       }
-      __syncthreads();  // partial sums complete
-
-      // ---- per target: sum the column groups, scale, rotate, carry (float-float) ----
-      if (tid < kTcTT) {
-        const int t = tid;
-        float sx = 0.f, sy = 0.f;
-#pragma unroll
-        for (int c = 0; c < CG; ++c) {
-          const float2 v = part[c * kTcTT + t];
-          sx += v.x;
-          sy += v.y;
-        }
-        const float sc = tsc[t];
-        const float re = sx * sc;
-        const float im = sgn * sy * sc;
-        float sr, cr;
-        __sincosf(tph[t], &sr, &cr);
-        float4 a = acc[t];
-        float h, e;
-        two_sum(a.x, fmaf(re, cr, -im * sr), h, e);  // h + e: the exact sum
-        a.x = h;
-        a.y = __fadd_rn(a.y, e);
-        two_sum(a.z, fmaf(re, sr, im * cr), h, e);
-        a.z = h;
-        a.w = __fadd_rn(a.w, e);
-        acc[t] = a;
-      }
-      __syncthreads();  // operands, partials and per-target data are rewritten next tile
     }
+    // the last tile's partial sums, once every consumer has written them
+    __syncthreads();
+    if (tid < kTcTT && se > sb && !*abort_flag) carry(se - 1);
 
     for (int t = tid; t < kTcTT; t += kTcThreads) {
       const int ti = tt * kTcTT + t;
