@@ -582,7 +582,9 @@ static int tc_fallback(int v) {
 
 std::vector<int> split_preferences(size_t N, size_t M) {
   (void)N;
-  if (M < 1024) return {3, 4};
+  // fewer targets than one 1024-target tile: the tensor-core builds' 512-target tiles
+  // waste no more than variant 3's, then the CUDA-core model 0 on 512 and 256
+  if (M < 1024) return {34, 44, 45, 3, 4};
   // fastest first: the tensor-core phase (pair model 3) on source tiles of 1024,
   // 512 and 256 (measured on the config-2 y pass: 2.87, 2.66, 2.38e12 pairs/s), then
   // the CUDA-core pair models 2, 1, 0 on ever smaller tiles
