@@ -262,6 +262,43 @@ def test_cli_generated_mode(holo, tmp_path):
         assert zf.size == 1024 and np.max(np.abs(zf - za)) < 1e-4
 
 
+def test_batched_short_source_tile_groups(holo, orc):
+    """Closer planes need narrower tile pairs: 10 um sources 0.2-0.35 m above a 128^2 grid of
+    7.56 um select the tensor-core builds with 256- and 512-source tiles and the 1024-source
+    one, and a wide set at 0.2 m a CUDA-core variant; one batch holds the four groups, each
+    drained by its own work-queue kernel (the short-tile builds keep two partial-sum
+    buffers per tile parity)."""
+    import torch
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(31)
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+    v = grid(128, 7.56e-6, 0.0)
+    cases, planned = [], set()
+    for ns, z0, sign in ((4096, 0.2, -1), (16384, 0.25, 1), (4096, 0.35, -1),
+                         (40000, 0.2, 1)):
+        u = grid(int(math.ceil(math.sqrt(ns))), 10e-6, z0)[:ns]
+        with holo.Plan(u, v, "split32") as pl:
+            planned.add(pl.info()["variant"])
+        amp, phase = rng.uniform(0, 1, ns), rng.uniform(0, 2 * np.pi, ns)
+        cases.append((amp, phase, u, sign))
+    tc_short = {var["variant"] for var in holo.variants("split32")
+                if var["pair_loop"] == 3 and var["source_tile"] in (256, 512)}
+    assert tc_short <= planned, (planned, "these geometries no longer select the short-tile "
+                                          "tensor-core builds")
+    probs = [holo.Problem(T(a), T(p), T(u), T(v), s, LAM,
+                          torch.zeros(2 * len(v), dtype=torch.float64, device=dev))
+             for a, p, u, s in cases]
+    with holo.Batch(probs, "split32") as b:
+        b.execute()
+        torch.cuda.synchronize()
+        b.execute()
+        torch.cuda.synchronize()
+    idx = np.arange(0, len(v), 61)
+    for pb, (amp, phase, u, sign) in zip(probs, cases):
+        yb = pb.y.cpu().numpy().view(np.complex128)
+        assert rel_l2(yb[idx], orc.transform_subset(amp, phase, u, v, idx, sign, LAM)) < 1e-5
+
+
 def test_batched_mixed_geometry_groups(holo, orc):
     """Problems of one batch keep the variant their own plan picks: 64^2 -> 128^2 grids of
     27 um pitch 0.35 m apart need the smallest tiles (256 targets x 256 sources) and the
