@@ -25,6 +25,8 @@ SPLIT32 = 1
 FORWARDS = 1
 BACKWARDS = -1
 FLAG_CONST_PHASE = 0x1
+TILE_HILBERT = 0  # tilings of holo_tile_order / holo_plan_tiling
+TILE_PACKED = 1
 
 _c = ctypes
 _dp = _c.c_void_p  # device or host pointer
@@ -54,6 +56,8 @@ SIGNATURES = {
     "holo_plan_execute": (_i, [_vp, _i, _d, _dp, _dp, _dp, _vp]),
     "holo_plan_execute_flags": (_i, [_vp, _i, _d, _dp, _dp, _dp, _i, _vp]),
     "holo_plan_get_order": (_i, [_vp, _i, _vp]),
+    "holo_plan_tiling": (_i, [_vp, _c.POINTER(_i), _c.POINTER(_i)]),
+    "holo_tile_order": (_i, [_vp, _dp, _sz, _i, _vp, _vp]),
     "holo_plan_info": (_i, [_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)]),
     "holo_plan_error_bound": (_i, [_vp, _c.POINTER(_d)]),
     "holo_transform_mc": (_i, [_vp, _i, _d, _dp, _dp, _dp, _sz, _dp, _sz, _dp, _c.c_uint64, _i,

@@ -184,6 +184,25 @@ def _device_of(*bufs: _Buf) -> int:
 
 
 # ---- one-shot transforms ------------------------------------------------------------
+_TILINGS = {N.TILE_HILBERT: "hilbert", N.TILE_PACKED: "packed"}
+
+
+def tile_order(points, tiling: str = "hilbert") -> np.ndarray:
+    """Tile order of a point set (xyz triples, NumPy or torch): order[i] = input index
+    of the i-th point in tile order, by the Hilbert or the packed tiling."""
+    codes = {v: k for k, v in _TILINGS.items()}
+    if tiling not in codes:
+        raise ValueError(f"tiling must be one of {sorted(codes)}")
+    b = _Buf(points, name="points")
+    if b.n % 3:
+        raise ValueError("points must hold xyz triples")
+    n = b.n // 3
+    h = handle(_device_of(b))
+    out = np.zeros(max(n, 1), np.int32)
+    N.check(h.lib.holo_tile_order(h.h, b.ptr, n, codes[tiling], out.ctypes.data, _stream(b)))
+    return out[:n]
+
+
 def transform(amp, phase, u, v, sign: int, lam: float = DEFAULT_LAMBDA, precision="split32",
               variant: int | None = None, flags: int = 0):
     """y_m = sum_n a_n exp(i(phi_n + sign k r_nm)) / r_nm for every target (complex)."""
@@ -343,6 +362,12 @@ class Plan:
         N.check(self.h.lib.holo_plan_adjoint(self.p, _sign(sign), lam, a.ptr, p.ptr, g.ptr,
                                              gaptr, gpptr, _stream(a)))
         return ga, gp
+
+    def tiling(self) -> dict:
+        """The tiling of the plan's sources and targets: "hilbert" or "packed"."""
+        ts, tt = ctypes.c_int(), ctypes.c_int()
+        N.check(self.h.lib.holo_plan_tiling(self.p, ctypes.byref(ts), ctypes.byref(tt)))
+        return {"sources": _TILINGS[ts.value], "targets": _TILINGS[tt.value]}
 
     def order(self, which: int) -> np.ndarray:
         n = self.n if which == 0 else self.m

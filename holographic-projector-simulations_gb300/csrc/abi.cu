@@ -188,23 +188,32 @@ void plan_release(holo_plan_s *p, cudaStream_t s) {
   delete p;
 }
 
-// Sort a point set into tile order (the order does not depend on the tile size).
-static int sort_set(holo_plan_s *p, const double *pos, int n, int n_pad, double **pos_sorted,
-                    int32_t **order, cudaStream_t s) {
-  HOLO_TRY(alloc_plan(p, (void **)pos_sorted, (size_t)3 * std::max(n_pad, 1) * sizeof(double), s));
-  HOLO_TRY(alloc_plan(p, (void **)order, (size_t)std::max(n, 1) * sizeof(int32_t), s));
-  if (n == 0) return launch_gather_pos(pos, nullptr, 0, n_pad, *pos_sorted, s);
+// Tile order of a point set into the plan's buffers (the order does not depend on
+// the tile size), or `known`, the order another plan computed for the same array.
+static int order_set(holo_plan_s *p, const double *pos, int n, int n_pad, double *pos_sorted,
+                     int32_t *order, cudaStream_t s, const int32_t *known, int tiling) {
+  if (n == 0) return launch_gather_pos(pos, nullptr, 0, n_pad, pos_sorted, s);
+  if (known) {
+    HOLO_CUDA(cudaMemcpyAsync(order, known, (size_t)n * sizeof(int32_t),
+                              cudaMemcpyDeviceToDevice, s));
+    return launch_gather_pos(pos, order, n, n_pad, pos_sorted, s);
+  }
   Scratch tmp(p->h, s);
-  double *bbox = tmp.get<double>(6);
-  double *bscr = tmp.get<double>(6 * 1024);
-  uint16_t *keys = tmp.get<uint16_t>(n);
   const size_t hist_n = sort_hist_entries(n);
-  uint32_t *hist = tmp.get<uint32_t>(hist_n);
-  uint32_t *scan = tmp.get<uint32_t>(hist_n + 4096 + 16);
-  if (!bbox || !bscr || !keys || !hist || !scan) return fail(HOLO_ERR_ALLOC, "tiler scratch");
-  HOLO_TRY(launch_bbox(pos, n, bbox, bscr, 1024, s));
-  HOLO_TRY(sort_points(pos, n, bbox, *order, keys, hist, scan, s));
-  HOLO_TRY(launch_gather_pos(pos, *order, n, n_pad, *pos_sorted, s));
+  TileScratch t{};
+  t.bbox = tmp.get<double>(6);
+  t.bbox_scratch = tmp.get<double>(6 * 1024);
+  t.keys = tmp.get<uint16_t>(n);
+  t.keys2 = tmp.get<uint16_t>(n);
+  t.hist = tmp.get<uint32_t>(hist_n);
+  t.scan = tmp.get<uint32_t>(hist_n + 4096 + 16);
+  t.tmp_a = tmp.get<int32_t>(n);
+  t.tmp_b = tmp.get<int32_t>(n);
+  if (!t.bbox || !t.bbox_scratch || !t.keys || !t.keys2 || !t.hist || !t.scan || !t.tmp_a ||
+      !t.tmp_b)
+    return fail(HOLO_ERR_ALLOC, "tiler scratch");
+  HOLO_TRY(tile_order(pos, n, order, t, s, tiling));
+  HOLO_TRY(launch_gather_pos(pos, order, n, n_pad, pos_sorted, s));
   return HOLO_OK;
 }
 
@@ -292,7 +301,9 @@ static int tile_error_bound(holo_plan_s *p, int cs, int tt, double *bound, doubl
 
 
 int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, size_t M,
-                     int precision, int forced_variant, cudaStream_t s, holo_plan_s **out) {
+                     int precision, int forced_variant, cudaStream_t s, holo_plan_s **out,
+                     const int32_t *known_order_s, const int32_t *known_order_t,
+                     int known_tiling_s, int known_tiling_t) {
   if (precision != HOLO_FP64 && precision != HOLO_SPLIT32)
     return fail(HOLO_ERR_INVALID, "unknown precision %d", precision);
   HOLO_TRY(check_sizes(N, M));
@@ -316,10 +327,20 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
     // sort once; pad sources to a multiple of every source tile size (3072 =
     // lcm of 1024 and 768; the others divide 1024)
     p->n_pad = std::max<int>(1, (int)((N + 3071) / 3072)) * 3072;
-    HOLO_TRY(sort_set(p.get(), u, (int)N, p->n_pad, &p->pos_s, &p->order_s, s));
-    HOLO_TRY(sort_set(p.get(), v, (int)M, (int)M, &p->pos_t, &p->order_t, s));
-    HOLO_TRY(alloc_plan(p.get(), (void **)&p->tiles_s, (size_t)6 * (N / 256 + 1) * sizeof(double), s));
-    HOLO_TRY(alloc_plan(p.get(), (void **)&p->tiles_t, (size_t)6 * (M / 256 + 1) * sizeof(double), s));
+    holo_plan_s *pp = p.get();
+    HOLO_TRY(alloc_plan(pp, (void **)&p->pos_s, (size_t)3 * p->n_pad * sizeof(double), s));
+    HOLO_TRY(alloc_plan(pp, (void **)&p->order_s, std::max<size_t>(N, 1) * sizeof(int32_t), s));
+    HOLO_TRY(alloc_plan(pp, (void **)&p->pos_t, (size_t)3 * std::max<size_t>(M, 1) * sizeof(double), s));
+    HOLO_TRY(alloc_plan(pp, (void **)&p->order_t, std::max<size_t>(M, 1) * sizeof(int32_t), s));
+    HOLO_TRY(alloc_plan(pp, (void **)&p->tiles_s, (size_t)6 * (N / 256 + 1) * sizeof(double), s));
+    HOLO_TRY(alloc_plan(pp, (void **)&p->tiles_t, (size_t)6 * (M / 256 + 1) * sizeof(double), s));
+    auto order_both = [&](int tiling, const int32_t *ks, const int32_t *kt) -> int {
+      HOLO_TRY(order_set(pp, u, (int)N, p->n_pad, p->pos_s, p->order_s, s, ks, tiling));
+      HOLO_TRY(order_set(pp, v, (int)M, (int)M, p->pos_t, p->order_t, s, kt, tiling));
+      p->tiling_s = ks ? known_tiling_s : tiling;
+      p->tiling_t = kt ? known_tiling_t : tiling;
+      return HOLO_OK;
+    };
     // candidates: a forced variant alone; else the variant tuned for this size
     // bucket, then the preference list (fastest first, ever smaller tiles); the
     // first whose path-length error bound holds is taken (sparse, wide or close
@@ -331,25 +352,45 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
       if (h->variant_table[precision][bucket] >= 0) cands.push_back(h->variant_table[precision][bucket]);
       for (int c : split_preferences(N, M)) cands.push_back(c);
     }
-    int shape_tt = -1, shape_cs = -1;
-    double mb[4] = {0.0, 0.0, 0.0, 0.0};
-    for (size_t i = 0; i < cands.size(); ++i) {
-      const Variant C = split_variant(cands[i]);
-      if (C.tt() != shape_tt || C.cs != shape_cs) {
-        // tile boxes of this shape (left in tiles_s / tiles_t) and its error model
-        double bound = 0.0, curv = 0.0, lin = 0.0, gemm = 0.0;
-        HOLO_TRY(tile_error_bound(p.get(), C.cs, C.tt(), &bound, &curv, &lin, &gemm, s));
-        mb[0] = bound;
-        mb[1] = bound + curv;
-        mb[2] = mb[1] + lin;
-        mb[3] = mb[2] + gemm;
-        shape_tt = C.tt();
-        shape_cs = C.cs;
+    // the first candidate whose bound holds on the current tiles (else the last);
+    // leaves that candidate's tile boxes in tiles_s / tiles_t
+    auto choose = [&](size_t *chosen) -> int {
+      int shape_tt = -1, shape_cs = -1;
+      double mb[4] = {0.0, 0.0, 0.0, 0.0};
+      for (size_t i = 0; i < cands.size(); ++i) {
+        const Variant C = split_variant(cands[i]);
+        if (C.tt() != shape_tt || C.cs != shape_cs) {
+          double bound = 0.0, curv = 0.0, lin = 0.0, gemm = 0.0;
+          HOLO_TRY(tile_error_bound(pp, C.cs, C.tt(), &bound, &curv, &lin, &gemm, s));
+          mb[0] = bound;
+          mb[1] = bound + curv;
+          mb[2] = mb[1] + lin;
+          mb[3] = mb[2] + gemm;
+          shape_tt = C.tt();
+          shape_cs = C.cs;
+        }
+        variant = cands[i];
+        *chosen = i;
+        for (int m = 0; m < 4; ++m) p->model_bounds[m] = mb[m];
+        p->err_bound = mb[C.model];
+        if (p->err_bound <= kSplitBoundMetres) break;
       }
-      variant = cands[i];
-      for (int m = 0; m < 4; ++m) p->model_bounds[m] = mb[m];
-      p->err_bound = mb[C.model];
-      if (p->err_bound <= kSplitBoundMetres) break;
+      return HOLO_OK;
+    };
+    // Hilbert tiles first (cheap); where their bound rules out the first candidate,
+    // the packed tiles (narrower for most point counts) get a second try, and the
+    // tiling that admits the earlier candidate is kept
+    size_t ci = 0;
+    HOLO_TRY(order_both(kTileHilbert, known_order_s, known_order_t));
+    HOLO_TRY(choose(&ci));
+    if (ci > 0 && forced_variant < 0) {
+      size_t cp = 0;
+      HOLO_TRY(order_both(kTilePacked, nullptr, nullptr));
+      HOLO_TRY(choose(&cp));
+      if (cp >= ci) {  // no gain: back to the Hilbert tiles
+        HOLO_TRY(order_both(kTileHilbert, nullptr, nullptr));
+        HOLO_TRY(choose(&ci));
+      }
     }
   }
   const Variant V = precision == HOLO_SPLIT32 ? split_variant(variant) : fp64_variant(variant);
@@ -677,6 +718,50 @@ int holo_plan_error_bound(holo_plan p, double *metres) {
   return HOLO_OK;
 }
 
+int holo_plan_tiling(holo_plan p, int *tiling_sources, int *tiling_targets) {
+  if (!p) return fail(HOLO_ERR_INVALID, "null plan");
+  if (tiling_sources) *tiling_sources = p->tiling_s;
+  if (tiling_targets) *tiling_targets = p->tiling_t;
+  return HOLO_OK;
+}
+
+int holo_tile_order(holo_handle h, const double *xyz, size_t n, int tiling, int32_t *order,
+                    holo_stream_t stream) {
+  if (!h) return fail(HOLO_ERR_INVALID, "null handle");
+  if (tiling != HOLO_TILE_HILBERT && tiling != HOLO_TILE_PACKED)
+    return fail(HOLO_ERR_INVALID, "unknown tiling %d", tiling);
+  if (n && (!xyz || !order)) return fail(HOLO_ERR_INVALID, "null point or order array");
+  HOLO_TRY(check_sizes(n, 0));
+  if (n == 0) return HOLO_OK;
+  std::lock_guard<std::mutex> lk(h->mu);
+  DeviceGuard g(h->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  bool dev = false;
+  HOLO_TRY(classify_all({xyz}, &dev));
+  Staged st(h, s);
+  const double *dxyz = xyz;
+  if (!dev) HOLO_TRY(st.up(xyz, 3 * n, &dxyz));
+  Scratch tmp(h, s);
+  const size_t hist_n = sort_hist_entries((int)n);
+  TileScratch t{};
+  t.bbox = tmp.get<double>(6);
+  t.bbox_scratch = tmp.get<double>(6 * 1024);
+  t.keys = tmp.get<uint16_t>(n);
+  t.keys2 = tmp.get<uint16_t>(n);
+  t.hist = tmp.get<uint32_t>(hist_n);
+  t.scan = tmp.get<uint32_t>(hist_n + 4096 + 16);
+  t.tmp_a = tmp.get<int32_t>(n);
+  t.tmp_b = tmp.get<int32_t>(n);
+  int32_t *dorder = tmp.get<int32_t>(n);
+  if (!t.bbox || !t.bbox_scratch || !t.keys || !t.keys2 || !t.hist || !t.scan || !t.tmp_a ||
+      !t.tmp_b || !dorder)
+    return fail(HOLO_ERR_ALLOC, "tiler scratch");
+  HOLO_TRY(tile_order(dxyz, (int)n, dorder, t, s, tiling));
+  HOLO_CUDA(cudaMemcpyAsync(order, dorder, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  HOLO_CUDA(cudaStreamSynchronize(s));
+  return HOLO_OK;
+}
+
 int holo_plan_get_order(holo_plan p, int which, int32_t *out) {
   if (!p || !out) return fail(HOLO_ERR_INVALID, "null plan or output");
   const int n = which == 0 ? p->N : p->M;
@@ -815,7 +900,8 @@ static int adjoint_impl(holo_plan_s *p, int sign, double lambda, const double *a
   if (p->N == 0) return HOLO_OK;
   if (!p->transposed)
     HOLO_TRY(plan_create_impl(p->h, p->v_orig, p->M, p->u_orig, p->N, p->precision, -1, s,
-                              &p->transposed));
+                              &p->transposed, p->order_t, p->order_s, p->tiling_t,
+                              p->tiling_s));
   Scratch tmp(p->h, s);
   double *g_amp = tmp.get<double>(std::max(p->M, 1));
   double *g_phase = tmp.get<double>(std::max(p->M, 1));
@@ -929,9 +1015,14 @@ static int project_dev(holo_handle h, double lambda, const double *xa, const dou
   if (!y || !mx || !partials) return fail(HOLO_ERR_ALLOC, "project scratch");
   holo_plan_s *p1 = nullptr;
   HOLO_TRY(plan_create_impl(h, u, N, v, M, precision, -1, s, &p1));
-  int rc = plan_execute_impl(p1, HOLO_BACKWARDS, lambda, xa, xp, y, 0, s);
-  plan_release(p1, s);
-  HOLO_TRY(rc);
+  // p1 lives until the reference-wave and z plans have taken its tile order of v
+  std::unique_ptr<holo_plan_s, void (*)(holo_plan_s *)> keep(p1, [](holo_plan_s *q) {
+    plan_release(q, q->last_stream);
+  });
+  const int32_t *order_v = precision == HOLO_SPLIT32 ? p1->order_t : nullptr;
+  const int tiling_v = p1->tiling_t;
+  HOLO_TRY(plan_execute_impl(p1, HOLO_BACKWARDS, lambda, xa, xp, y, 0, s));
+  int rc = HOLO_OK;
   if (!reference_wave) {
     HOLO_TRY(normalize_polar_dev(h, y, M, ya, yp, mx, s));
   } else {
@@ -948,7 +1039,8 @@ static int project_dev(holo_handle h, double lambda, const double *xa, const dou
     const double host_src[5] = {0.0, 0.0, vz - reference_distance, 1.0, 0.0};  // xyz, amp, phase
     HOLO_CUDA(cudaMemcpyAsync(src, host_src, sizeof(host_src), cudaMemcpyHostToDevice, s));
     holo_plan_s *pr = nullptr;
-    HOLO_TRY(plan_create_impl(h, src, 1, v, M, precision, -1, s, &pr));
+    HOLO_TRY(plan_create_impl(h, src, 1, v, M, precision, -1, s, &pr, nullptr, order_v,
+                              holo::kTileHilbert, tiling_v));
     rc = plan_execute_impl(pr, HOLO_FORWARDS, lambda, src + 3, src + 4, yref, 0, s);
     plan_release(pr, s);
     HOLO_TRY(rc);
@@ -961,7 +1053,7 @@ static int project_dev(holo_handle h, double lambda, const double *xa, const dou
   double2 *z = tmp.get<double2>(P);
   if (!z) return fail(HOLO_ERR_ALLOC, "project scratch");
   holo_plan_s *p2 = nullptr;
-  HOLO_TRY(plan_create_impl(h, v, M, w, P, precision, -1, s, &p2));
+  HOLO_TRY(plan_create_impl(h, v, M, w, P, precision, -1, s, &p2, order_v, nullptr, tiling_v));
   rc = plan_execute_impl(p2, HOLO_FORWARDS, lambda, ya, yp, z, 0, s);
   plan_release(p2, s);
   HOLO_TRY(rc);

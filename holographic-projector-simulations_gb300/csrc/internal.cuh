@@ -29,8 +29,9 @@ constexpr double kTwoPiHi = 6.283185307179586232;
 constexpr double kTwoPiLo = 2.4492935982947064e-16;
 constexpr double kInvTwoPi = 0.15915494309189533577;
 
-constexpr int kHilbertGrid = 64;                 // cells per axis of the tiling sort
-constexpr int kCells = kHilbertGrid * kHilbertGrid;
+constexpr int kCells = 4096;                     // bins of the tiler's counting sorts
+constexpr int kSuperTile = 8192;                 // points bisected together in shared memory
+constexpr int kLeafTile = 256;                   // smallest tile of the bisection
 constexpr int kSortBlock = 4096;                 // points per block of the counting sort
 constexpr long long kWaitCycles = 4000000000LL;  // bounded device wait (~2 s at 2 GHz)
 
@@ -175,9 +176,23 @@ void note_launches(int n);
 // tiler.cu
 int launch_bbox(const double *pos, int n, double *bbox6, double *scratch, int scratch_blocks,
                 cudaStream_t s);
-int sort_points(const double *pos, int n, const double *bbox6, int32_t *order, uint16_t *keys,
-                uint32_t *hist, uint32_t *scan_tmp, cudaStream_t s);
 size_t sort_hist_entries(int n);
+// Device scratch of tile_order for n points: bbox[6], bbox_scratch[6 * 1024],
+// keys and keys2[n], hist[sort_hist_entries(n)], scan[that + 4096 + 16], tmp_a and
+// tmp_b[n].
+struct TileScratch {
+  double *bbox, *bbox_scratch;
+  uint16_t *keys, *keys2;
+  uint32_t *hist, *scan;
+  int32_t *tmp_a, *tmp_b;
+};
+// Tile order of a point set (pos: n xyz triples): order[r] = input index of the
+// r-th point; tiles of 256, 512 and 1024 consecutive points are spatially compact.
+// tiling: kTileHilbert (needs bbox, bbox_scratch, keys, hist, scan of the scratch)
+// or kTilePacked (all of it; none for n <= kSuperTile).
+constexpr int kTileHilbert = 0, kTilePacked = 1;
+int tile_order(const double *pos, int n, int32_t *order, const TileScratch &t, cudaStream_t s,
+               int tiling);
 int launch_gather_pos(const double *pos, const int32_t *order, int n, int n_pad, double *out,
                       cudaStream_t s);
 int launch_tile_bbox(const double *pos_sorted, int n, int tile, double *tiles, cudaStream_t s);
@@ -258,6 +273,7 @@ struct holo_plan_s {
   int n_stiles = 0, n_ttiles = 0;
   double err_bound = 0.0;        // split path: bound on the path-length error (m)
   double model_bounds[4] = {0.0, 0.0, 0.0, 0.0};  // the same for pair models 0-3 (same tiles)
+  int tiling_s = holo::kTileHilbert, tiling_t = holo::kTileHilbert;  // split: each set's tiling
   cudaStream_t last_stream = nullptr;
   // device buffers
   double *pos_s = nullptr;       // 3 * n_pad
@@ -289,9 +305,13 @@ namespace holo {
 void *pool_alloc(holo_handle h, size_t bytes, cudaStream_t s);
 void pool_free(void *p, cudaStream_t s);
 int size_bucket(size_t N, size_t M);
+// known_order_s / known_order_t: the tile order of the same source / target array
+// from another split plan (copied instead of recomputed), of tiling known_tiling_s/t
 int plan_create_impl(holo_handle h, const double *u_dev, size_t N, const double *v_dev,
                      size_t M, int precision, int forced_variant, cudaStream_t s,
-                     holo_plan_s **out);
+                     holo_plan_s **out, const int32_t *known_order_s = nullptr,
+                     const int32_t *known_order_t = nullptr, int known_tiling_s = kTileHilbert,
+                     int known_tiling_t = kTileHilbert);
 int plan_execute_impl(holo_plan_s *p, int sign, double lambda, const double *amp_dev,
                       const double *phase_dev, double2 *y_dev, int flags, cudaStream_t s);
 void plan_release(holo_plan_s *p, cudaStream_t s);

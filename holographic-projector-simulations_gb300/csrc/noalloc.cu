@@ -169,11 +169,12 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
   const size_t shared_off = cv.off;  // sort scratch first, partial sums later
   const size_t nmax = std::max(N, M);
   const size_t hist_n = sort_hist_entries((int)nmax);
-  double *bbox = cv.take<double>(6);
-  double *bscr = cv.take<double>(6 * 1024);
-  uint16_t *keys = cv.take<uint16_t>(nmax);
-  uint32_t *hist = cv.take<uint32_t>(hist_n);
-  uint32_t *scan = cv.take<uint32_t>(hist_n + 4096 + 16);
+  TileScratch ts{};  // the Hilbert tiling: the cheaper sort, and its smaller scratch
+  ts.bbox = cv.take<double>(6);
+  ts.bbox_scratch = cv.take<double>(6 * 1024);
+  ts.keys = cv.take<uint16_t>(nmax);
+  ts.hist = cv.take<uint32_t>(hist_n);
+  ts.scan = cv.take<uint32_t>(hist_n + 4096 + 16);
   const size_t sort_end = cv.off;
   const size_t partial_min = align256(M * sizeof(double2));  // one split: written to y directly
   const size_t need = std::max(sort_end, shared_off);
@@ -184,11 +185,9 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
 
   HOLO_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));  // the error word starts at zero
   // ---- tile order of both point sets ----
-  HOLO_TRY(launch_bbox(u, (int)N, bbox, bscr, 1024, s));
-  HOLO_TRY(sort_points(u, (int)N, bbox, order_s, keys, hist, scan, s));
+  HOLO_TRY(tile_order(u, (int)N, order_s, ts, s, kTileHilbert));
   HOLO_TRY(launch_gather_pos(u, order_s, (int)N, n_pad, pos_s, s));
-  HOLO_TRY(launch_bbox(v, (int)M, bbox, bscr, 1024, s));
-  HOLO_TRY(sort_points(v, (int)M, bbox, order_t, keys, hist, scan, s));
+  HOLO_TRY(tile_order(v, (int)M, order_t, ts, s, kTileHilbert));
   HOLO_TRY(launch_gather_pos(v, order_t, (int)M, (int)M, pos_t, s));
 
   // ---- kernel: the planner's preference list, first whose error bound holds ----

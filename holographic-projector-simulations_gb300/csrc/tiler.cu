@@ -1,12 +1,21 @@
 // tiler.cu -- spatial tiling of a point set on the device.
 //
-// The split-precision kernel needs every tile of consecutive points to be
-// spatially compact (its FP32 arithmetic is relative to the tile centre).  The
+// The split-precision kernels need every tile of consecutive points to be
+// spatially compact: their FP32 arithmetic is relative to the tile centre, and
+// the planner's error bound grows with the square of the widest tile.  The
 // reference keeps points in file order (its square-tile reorder,
-// cuda/reorder.cu:1-92, is never called); here points are sorted by the
-// Hilbert index of a 64 x 64 cell grid over the two widest axes of the
-// bounding box, with a stable counting sort (deterministic: equal keys keep
-// their input order).  Tiles are then fixed-size ranges of the sorted order.
+// cuda/reorder.cu:1-92, is never called).  Two tilings:
+//   Hilbert: one stable counting sort by the Hilbert index of a 64 x 64 cell grid
+//     over the two widest axes -- cheap, and exact squares on power-of-two grids,
+//     but runs of the curve can be L-shaped or long for other point counts;
+//   packed: super tiles of 8192 by sort-tile-recursive strips (stable counting
+//     sorts by the quantised widest axis, then the second axis, then the strip),
+//     each bisected in shared memory down to tiles of 256 by splitting off
+//     power-of-two prefixes, so every tile of 256, 512 or 1024 points is one
+//     bisection segment of nearly square extent -- about twice the planning
+//     time, used where the Hilbert tiles' error bound rules out the fastest kernel.
+// All sorts are stable and ties keep input order: each order is deterministic
+// and does not depend on the tile size.
 #include <float.h>
 
 #include "internal.cuh"
@@ -75,6 +84,9 @@ __global__ void __launch_bounds__(256) k_bbox_final(const double *__restrict__ p
     }
 }
 
+constexpr int kHilbertCells = 64;  // cells per axis of the Hilbert tiling (kCells in all)
+static_assert(kHilbertCells * kHilbertCells == kCells, "Hilbert cells fill the sort's bins");
+
 // Hilbert index of cell (x, y) on an n x n grid (n a power of two): the
 // classic quadrant-rotation construction of the curve.
 __device__ __forceinline__ uint32_t hilbert_xy2d(int n, int x, int y) {
@@ -106,16 +118,277 @@ __global__ void __launch_bounds__(256) k_cell_keys(const double *__restrict__ po
   if (ext[a1] > ext[a0]) { int t = a0; a0 = a1; a1 = t; }
   if (ext[a2] > ext[a1]) { int t = a1; a1 = a2; a2 = t; }
   if (ext[a1] > ext[a0]) { int t = a0; a0 = a1; a1 = t; }
-  const double s0 = ext[a0] > 0 ? kHilbertGrid / ext[a0] : 0.0;
-  const double s1 = ext[a1] > 0 ? kHilbertGrid / ext[a1] : 0.0;
+  const double s0 = ext[a0] > 0 ? kHilbertCells / ext[a0] : 0.0;
+  const double s1 = ext[a1] > 0 ? kHilbertCells / ext[a1] : 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double *p = pos + 3 * (size_t)i;
     int cx = (int)((p[a0] - bbox[a0]) * s0);
     int cy = (int)((p[a1] - bbox[a1]) * s1);
-    cx = min(max(cx, 0), kHilbertGrid - 1);
-    cy = min(max(cy, 0), kHilbertGrid - 1);
-    keys[i] = (uint16_t)hilbert_xy2d(kHilbertGrid, cx, cy);
+    cx = min(max(cx, 0), kHilbertCells - 1);
+    cy = min(max(cy, 0), kHilbertCells - 1);
+    keys[i] = (uint16_t)hilbert_xy2d(kHilbertCells, cx, cy);
   }
+}
+
+// The two widest axes of a bounding box (lo[3], hi[3]), widest first.
+__device__ __forceinline__ void widest_axes(const double *bbox, int *a0, int *a1) {
+  double ext[3];
+  for (int d = 0; d < 3; ++d) ext[d] = bbox[3 + d] - bbox[d];
+  int x = 0, y = 1, z = 2;  // sort axes by extent, descending
+  if (ext[y] > ext[x]) { int t = x; x = y; y = t; }
+  if (ext[z] > ext[y]) { int t = y; y = z; z = t; }
+  if (ext[y] > ext[x]) { int t = x; x = y; y = t; }
+  *a0 = x;
+  *a1 = y;
+}
+
+// Points per strip: about sqrt(#super tiles / aspect) strips make the super tiles
+// square; the count is a multiple of the super tile so strips end on super-tile
+// boundaries.  Every thread computes the same value from the box.
+__device__ __forceinline__ long long strip_points(const double *bbox, int n) {
+  int a0, a1;
+  widest_axes(bbox, &a0, &a1);
+  const double e0 = bbox[3 + a0] - bbox[a0], e1 = bbox[3 + a1] - bbox[a1];
+  const long long nsup = (n + kSuperTile - 1) / kSuperTile;
+  const double aspect = e0 > 0.0 ? fmax(e1 / e0, 1e-9) : 1.0;
+  long long strips = llround(sqrt((double)nsup / aspect));
+  strips = max(1LL, min(strips, min(nsup, (long long)kCells)));
+  return (nsup + strips - 1) / strips * kSuperTile;
+}
+
+// Key of every point: its coordinate along the widest (axis 0) or the second widest
+// (axis 1) axis of the box, quantised to kCells bins.
+__global__ void __launch_bounds__(256) k_axis_keys(const double *__restrict__ pos, int n,
+                                                   const double *__restrict__ bbox, int which,
+                                                   uint16_t *__restrict__ keys) {
+  int a0, a1;
+  widest_axes(bbox, &a0, &a1);
+  const int a = which ? a1 : a0;
+  const double ext = bbox[3 + a] - bbox[a];
+  const double sc = ext > 0.0 ? kCells / ext : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int c = (int)((pos[3 * (size_t)i + a] - bbox[a]) * sc);
+    keys[i] = (uint16_t)min(max(c, 0), kCells - 1);
+  }
+}
+
+// strip[order_x[r]] = r / (points per strip): the strip of each point by its rank
+// along the widest axis.
+__global__ void __launch_bounds__(256) k_strip_keys(const int32_t *__restrict__ order_x, int n,
+                                                    const double *__restrict__ bbox,
+                                                    uint16_t *__restrict__ strip) {
+  const long long per = strip_points(bbox, n);
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    strip[order_x[r]] = (uint16_t)(r / per);
+}
+
+// out[r] = src[perm[r]]
+__global__ void __launch_bounds__(256) k_permute_keys(const uint16_t *__restrict__ src,
+                                                      const int32_t *__restrict__ perm, int n,
+                                                      uint16_t *__restrict__ out) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    out[r] = src[perm[r]];
+}
+
+// out[r] = a[b[r]]
+__global__ void __launch_bounds__(256) k_compose(const int32_t *__restrict__ a,
+                                                 const int32_t *__restrict__ b, int n,
+                                                 int32_t *__restrict__ out) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    out[r] = a[b[r]];
+}
+
+__device__ __forceinline__ uint32_t ordered_bits(float f) {
+  const uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float from_ordered_bits(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Segment holding position i of a super tile of nl points after `level` splits:
+// a segment longer than kLeafTile splits off its largest power-of-two prefix, so
+// every split point is a multiple of each smaller tile size (256, 512, 1024).
+__device__ __forceinline__ void bisect_segment(int i, int nl, int level, int *start, int *len) {
+  int s = 0, l = nl;
+  for (int k = 0; k < level && l > kLeafTile; ++k) {
+    const int unit = 1 << (31 - __clz(l - 1));  // largest power of two below l
+    if (i < s + unit) {
+      l = unit;
+    } else {
+      s += unit;
+      l -= unit;
+    }
+  }
+  *start = s;
+  *len = l;
+}
+
+// Compare-exchange of the bitonic network on a pair whose lower index is `lo_i`:
+// keep the smaller key at the lower index when (lo_i & k) == 0, else the larger.
+__device__ __forceinline__ uint64_t bitonic_keep(uint64_t mine, uint64_t other, bool lower,
+                                                 bool ascending) {
+  const uint64_t mn = mine < other ? mine : other, mx = mine < other ? other : mine;
+  return (lower == ascending) ? mn : mx;
+}
+
+// The in-register stages (partner distance J < 8) of the network below.
+template <int J>
+__device__ __forceinline__ void bitonic_reg_stage(uint64_t (&v)[8], int t, int k) {
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    if (e & J) continue;
+    const uint64_t a = v[e], b = v[e | J];
+    if ((a > b) == (((8 * t + e) & k) == 0)) {
+      v[e] = b;
+      v[e | J] = a;
+    }
+  }
+}
+
+// Bitonic sort of kSuperTile keys, 8 consecutive keys per thread (1024 threads):
+// partner distance j < 8 within a thread's registers, 8 <= j < 256 by warp
+// shuffles, j >= 256 through shared memory (element i at (i % 8) * 1024 + i / 8, so
+// a warp's accesses are consecutive).  Sorts each aligned block of kmax keys (a
+// power of two) ascending: the merge phases stop at kmax, whose phase runs
+// ascending everywhere.
+__device__ void bitonic_sort_8192(uint64_t (&v)[8], uint64_t *sh, int kmax) {
+  const int t = threadIdx.x;
+  for (int k = 2; k <= kmax; k <<= 1) {
+    const int kd = k == kmax ? 2 * kSuperTile : k;  // (i & kd) == 0: ascending
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 256) {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) sh[e * 1024 + t] = v[e];
+        __syncthreads();
+        const int pt = t ^ (j >> 3);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const int i = 8 * t + e;
+          v[e] = bitonic_keep(v[e], sh[e * 1024 + pt], (t & (j >> 3)) == 0, (i & kd) == 0);
+        }
+        __syncthreads();
+      } else if (j >= 8) {
+        const int m = j >> 3;  // partner lane offset (< 32)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const int i = 8 * t + e;
+          const uint64_t o = __shfl_xor_sync(0xffffffffu, v[e], m);
+          v[e] = bitonic_keep(v[e], o, (t & m) == 0, (i & kd) == 0);
+        }
+      } else if (j == 4) {
+        bitonic_reg_stage<4>(v, t, kd);
+      } else if (j == 2) {
+        bitonic_reg_stage<2>(v, t, kd);
+      } else {
+        bitonic_reg_stage<1>(v, t, kd);
+      }
+    }
+  }
+}
+
+// Recursive bisection of each super tile of kSuperTile consecutive points of
+// `order` (in place): at each of five levels every segment longer than kLeafTile
+// is sorted along the widest axis of its own box and split off at its largest
+// power-of-two prefix, so tiles of 256, 512 and 1024 points are each one segment,
+// of nearly square extent.  One bitonic sort of 64-bit keys (segment start,
+// coordinate, position) per level keeps segments in place and ties in order.
+__global__ void __launch_bounds__(1024) k_local_bisect(const double *__restrict__ pos, int n,
+                                                       int32_t *__restrict__ order) {
+  extern __shared__ __align__(16) unsigned char bsm[];
+  uint64_t *sh = reinterpret_cast<uint64_t *>(bsm);                     // [kSuperTile]
+  int32_t *idx = reinterpret_cast<int32_t *>(sh + kSuperTile);          // [2][kSuperTile]
+  __shared__ uint32_t box[kSuperTile / kLeafTile][6];                   // ordered min, max
+  __shared__ double ref[3];  // coordinates relative to the tile's first point, as floats
+  __shared__ int kmax;       // sort blocks of this level: each segment lies in one
+  const int t = threadIdx.x;
+  const int base = blockIdx.x * kSuperTile;
+  const int nl = min(kSuperTile, n - base);
+  for (int i = t; i < nl; i += blockDim.x) idx[i] = order[base + i];
+  if (t < 3) ref[t] = pos[3 * (size_t)order[base] + t];
+  int cur = 0;
+  for (int level = 0; level < 5; ++level) {
+    for (int c = t; c < (kSuperTile / kLeafTile) * 6; c += blockDim.x)
+      box[c / 6][c % 6] = (c % 6) < 3 ? 0xffffffffu : 0u;
+    if (t == 0) kmax = 2;
+    __syncthreads();
+    // a warp's 256 consecutive positions lie in one segment (segments longer than
+    // kLeafTile start at multiples of it): reduce in the warp, one atomic per warp
+    int st[8], ln[8];
+    uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0u, 0u, 0u};
+    int blk = 2;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = 8 * t + e;
+      st[e] = 0;
+      ln[e] = 0;
+      if (i >= nl) continue;
+      bisect_segment(i, nl, level, &st[e], &ln[e]);
+      // smallest aligned power-of-two block holding the whole segment
+      const int last = st[e] + ln[e] - 1;
+      const int b = ln[e] > 1 ? 2 << (31 - __clz(st[e] ^ last)) : 2;
+      blk = max(blk, b);
+      if (ln[e] > kLeafTile) {
+        const double *p = pos + 3 * (size_t)idx[cur * kSuperTile + i];
+        for (int d = 0; d < 3; ++d) {
+          const uint32_t o = ordered_bits((float)(p[d] - ref[d]));
+          mn[d] = min(mn[d], o);
+          mx[d] = max(mx[d], o);
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      for (int d = 0; d < 3; ++d) {
+        mn[d] = min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+        mx[d] = max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+      }
+      blk = max(blk, __shfl_xor_sync(0xffffffffu, blk, o));
+    }
+    if ((t & 31) == 0) {
+      const int i0 = 8 * t;  // the warp's first position
+      if (i0 < nl && ln[0] > kLeafTile)
+        for (int d = 0; d < 3; ++d) {
+          atomicMin(&box[st[0] / kLeafTile][d], mn[d]);
+          atomicMax(&box[st[0] / kLeafTile][3 + d], mx[d]);
+        }
+      atomicMax(&kmax, blk);
+    }
+    __syncthreads();
+    uint64_t v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = 8 * t + e;
+      uint64_t k = ~0ull;  // padding sorts last
+      if (i < nl) {
+        uint32_t c = 0;
+        if (ln[e] > kLeafTile) {
+          const uint32_t *b = box[st[e] / kLeafTile];
+          int a = 0;
+          float ext = -1.f;
+          for (int d = 0; d < 3; ++d) {
+            const float ed = from_ordered_bits(b[3 + d]) - from_ordered_bits(b[d]);
+            if (ed > ext) {
+              ext = ed;
+              a = d;
+            }
+          }
+          c = ordered_bits((float)(pos[3 * (size_t)idx[cur * kSuperTile + i] + a] - ref[a]));
+        }
+        k = ((uint64_t)st[e] << 45) | ((uint64_t)c << 13) | (uint64_t)i;
+      }
+      v[e] = k;
+    }
+    bitonic_sort_8192(v, sh, kmax);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = 8 * t + e;
+      if (i < nl)
+        idx[(cur ^ 1) * kSuperTile + i] = idx[cur * kSuperTile + (int)(v[e] & (kSuperTile - 1))];
+    }
+    cur ^= 1;
+    __syncthreads();
+  }
+  for (int i = t; i < nl; i += blockDim.x) order[base + i] = idx[cur * kSuperTile + i];
 }
 
 // Per-block histogram of cell keys, stored cell-major: hist[cell * nblk + blk].
@@ -344,12 +617,11 @@ size_t sort_hist_entries(int n) {
   return (nblk ? nblk : 1) * kCells;
 }
 
-int sort_points(const double *pos, int n, const double *bbox6, int32_t *order, uint16_t *keys,
-                uint32_t *hist, uint32_t *scan_tmp, cudaStream_t s) {
-  if (n <= 0) return HOLO_OK;
+// Stable counting sort of n keys (< kCells) into order (indices 0..n-1).
+static int counting_sort(const uint16_t *keys, int n, int32_t *order, uint32_t *hist,
+                         uint32_t *scan_tmp, cudaStream_t s) {
   const int nblk = (n + kSortBlock - 1) / kSortBlock;
   if (nblk > 4096) return fail(HOLO_ERR_INVALID, "point set too large for the tiler (%d)", n);
-  k_cell_keys<<<grid_for(n, 256, 4096), 256, 0, s>>>(pos, n, bbox6, keys); note_launches(1);
   k_hist<<<nblk, 256, 0, s>>>(keys, n, hist, nblk); note_launches(1);
   const size_t count = (size_t)nblk * kCells;
   const int nb = (int)((count + 4095) / 4096);  // == nblk
@@ -359,6 +631,38 @@ int sort_points(const double *pos, int n, const double *bbox6, int32_t *order, u
   k_scan_sums<<<1, 1024, 0, s>>>(sums, nb); note_launches(1);
   k_scan_add<<<nb, 1024, 0, s>>>(offsets, count, sums); note_launches(1);
   k_scatter<<<nblk, 32, 0, s>>>(keys, n, offsets, nblk, order); note_launches(1);
+  HOLO_CUDA(cudaGetLastError());
+  return HOLO_OK;
+}
+
+int tile_order(const double *pos, int n, int32_t *order, const TileScratch &t, cudaStream_t s,
+               int tiling) {
+  if (n <= 0) return HOLO_OK;
+  if (tiling == kTileHilbert) {
+    HOLO_TRY(launch_bbox(pos, n, t.bbox, t.bbox_scratch, 1024, s));
+    k_cell_keys<<<grid_for(n, 256, 4096), 256, 0, s>>>(pos, n, t.bbox, t.keys); note_launches(1);
+    return counting_sort(t.keys, n, order, t.hist, t.scan, s);
+  }
+  constexpr int kBisectSmem = kSuperTile * (8 + 2 * 4);
+  HOLO_TRY(kernel_setup<k_local_bisect>(1024, kBisectSmem, nullptr));
+  if (n <= kSuperTile) {
+    HOLO_TRY(launch_iota(order, n, s));
+  } else {
+    HOLO_TRY(launch_bbox(pos, n, t.bbox, t.bbox_scratch, 1024, s));
+    const int g = grid_for(n, 256, 8192);
+    // order along the widest axis -> each point's strip
+    k_axis_keys<<<g, 256, 0, s>>>(pos, n, t.bbox, 0, t.keys); note_launches(1);
+    HOLO_TRY(counting_sort(t.keys, n, t.tmp_a, t.hist, t.scan, s));
+    k_strip_keys<<<g, 256, 0, s>>>(t.tmp_a, n, t.bbox, t.keys2); note_launches(1);
+    // along the second axis, then (stably) by strip
+    k_axis_keys<<<g, 256, 0, s>>>(pos, n, t.bbox, 1, t.keys); note_launches(1);
+    HOLO_TRY(counting_sort(t.keys, n, t.tmp_b, t.hist, t.scan, s));
+    k_permute_keys<<<g, 256, 0, s>>>(t.keys2, t.tmp_b, n, t.keys); note_launches(1);
+    HOLO_TRY(counting_sort(t.keys, n, t.tmp_a, t.hist, t.scan, s));
+    k_compose<<<g, 256, 0, s>>>(t.tmp_b, t.tmp_a, n, order); note_launches(1);
+  }
+  k_local_bisect<<<(n + kSuperTile - 1) / kSuperTile, 1024, kBisectSmem, s>>>(pos, n, order);
+  note_launches(1);
   HOLO_CUDA(cudaGetLastError());
   return HOLO_OK;
 }

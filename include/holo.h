@@ -118,6 +118,25 @@ int holo_plan_info(holo_plan p, int *variant, int *splits, int *target_tile,
  * point sets' bounding boxes touch (near field: use HOLO_FP64). */
 int holo_plan_error_bound(holo_plan p, double *metres);
 
+/* ---- tilings (no counterpart in the reference: it keeps points in file order;
+ * its square-tile reorder, cuda/reorder.cu:1-92, is never called) ------------
+ * HOLO_TILE_HILBERT: one stable sort by the Hilbert index of a 64 x 64 cell grid
+ * over the two widest axes (cheap; exact squares on power-of-two grids).
+ * HOLO_TILE_PACKED: super tiles of 8192 points in strips, each bisected so that
+ * every tile of 256, 512 or 1024 consecutive points is nearly square (about twice
+ * the planning time; narrower tiles for most other point counts).
+ * A HOLO_SPLIT32 plan tiles with HOLO_TILE_HILBERT and tries HOLO_TILE_PACKED
+ * where the Hilbert tiles' error bound rules out the fastest kernel. */
+#define HOLO_TILE_HILBERT 0
+#define HOLO_TILE_PACKED 1
+/* Tile order of n points (xyz triples, device or host pointer): order[i] = input
+ * index of the i-th point in tile order (order: host pointer, n entries).  No
+ * reference counterpart. */
+int holo_tile_order(holo_handle h, const double *xyz, size_t n, int tiling, int32_t *order,
+                    holo_stream_t stream);
+/* The tiling a HOLO_SPLIT32 plan used for its sources and for its targets. */
+int holo_plan_tiling(holo_plan p, int *tiling_sources, int *tiling_targets);
+
 /* ---- Monte Carlo estimator (transform(), README.md:127; not in the snapshot)
  * Sources in tile order are cut into strata of `subsample` entries, targets in
  * tile order into blocks of `targets_per_block`.  Every block sums one source
