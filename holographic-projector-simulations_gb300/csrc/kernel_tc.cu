@@ -294,8 +294,33 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
           ah[d] = fr->ah[d];
           al[d] = fr->al[d];
         }
-        // the source rows of this thread: all computed, then all stored, so that
-        // their dependent chains interleave
+        // the target row and the source rows of this thread: all computed, then all
+        // stored, in one straight-line block so that their dependent chains interleave
+        // (with 512 consumers and 512 targets, and source tiles a multiple of 512,
+        // both guards below are compile-time true).  Source records past N are
+        // staged as zeros (offsets, phase and amplitude), from which the row comes
+        // out all zeros, as it must.
+        constexpr bool kAllTargets = NC <= kTcTT;  // every consumer thread owns a target
+        const bool has_t = kAllTargets || tid < kTcTT;
+        float f[kTcK], tph_v = 0.f, tsc_v = 0.f;
+        if (has_t) {
+          const int t = tid;
+          const float th[3] = {tgeo[t], tgeo[kTcTT + t], tgeo[2 * kTcTT + t]};
+          const float tl[3] = {tgeo[3 * kTcTT + t], tgeo[4 * kTcTT + t], tgeo[5 * kTcTT + t]};
+          float S, E, S2, E2;
+          dot3_ff(ah, al, th, tl, S, E);
+          two_sum(S, fr->b0h, S2, E2);
+          const float B = reduce_two_pi_ff(S2, __fadd_rn(__fadd_rn(E, E2), fr->b0l));
+          const float Tx = fmaf(f1x, th[0], fmaf(f1y, th[1], f1z * th[2]));
+          const float Ty = fmaf(f2x, th[0], fmaf(f2y, th[1], f2z * th[2]));
+          const float Qt = fr->r0f + fmaf(fex, th[0], fmaf(fey, th[1], fez * th[2]));
+          const float T2 = fmaf(Tx, Tx, Ty * Ty);
+          const float Iq = ak / Qt, Kq = Iq / Qt;
+          f[0] = Iq; f[1] = -2.f * Iq * Tx; f[2] = -2.f * Iq * Ty; f[3] = Kq * T2;
+          f[4] = Kq; f[5] = -2.f * Kq * Tx; f[6] = -2.f * Kq * Ty; f[7] = 0.f;
+          tph_v = B + sgn * Iq * T2;  // the target's rotation, incl. the Iq T2 term
+          tsc_v = Iq * iak;           // 1 / Qt
+        }
         constexpr int R = (kTcCS + NC - 1) / NC;
         static_assert(kTcCS % NC == 0 || NC % kTcCS == 0, "source rows per consumer thread");
         float g[R][kTcK], a3[R][3], am[R];
@@ -306,7 +331,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
           for (int k = 0; k < kTcK; ++k) g[r][k] = 0.f;
           a3[r][0] = a3[r][1] = a3[r][2] = 0.f;
           am[r] = 0.f;
-          if (i < kTcCS && j * kTcCS + i < P.N) {
+          if (kTcCS >= NC || i < kTcCS) {
             const float *q = raw_geo + 6 * i;
             const float sh[3] = {q[0], q[1], q[2]}, sl[3] = {q[3], q[4], q[5]};
             const float2 pa = raw_apf[i];
@@ -331,7 +356,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const int i = tid + r * NC;
-          if (i >= kTcCS) break;
+          if (kTcCS < NC && i >= kTcCS) break;
           store_row_split(opb_hi, opb_lo, i, g[r]);
           const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
           *reinterpret_cast<float4 *>(opb_a + tc_off(i, 0)) =
@@ -339,25 +364,10 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
           *reinterpret_cast<float4 *>(opb_a + tc_off(i, 4)) = z;
           amp[i] = am[r];
         }
-        // targets: one per consumer thread (the first kTcTT of them)
-        if (tid < kTcTT) {
-          const int t = tid;
-          const float th[3] = {tgeo[t], tgeo[kTcTT + t], tgeo[2 * kTcTT + t]};
-          const float tl[3] = {tgeo[3 * kTcTT + t], tgeo[4 * kTcTT + t], tgeo[5 * kTcTT + t]};
-          float S, E, S2, E2;
-          dot3_ff(ah, al, th, tl, S, E);
-          two_sum(S, fr->b0h, S2, E2);
-          const float B = reduce_two_pi_ff(S2, __fadd_rn(__fadd_rn(E, E2), fr->b0l));
-          const float Tx = fmaf(f1x, th[0], fmaf(f1y, th[1], f1z * th[2]));
-          const float Ty = fmaf(f2x, th[0], fmaf(f2y, th[1], f2z * th[2]));
-          const float Qt = fr->r0f + fmaf(fex, th[0], fmaf(fey, th[1], fez * th[2]));
-          const float T2 = fmaf(Tx, Tx, Ty * Ty);
-          const float Iq = ak / Qt, Kq = Iq / Qt;
-          const float f[kTcK] = {Iq, -2.f * Iq * Tx, -2.f * Iq * Ty, Kq * T2,
-                                 Kq, -2.f * Kq * Tx, -2.f * Kq * Ty, 0.f};
-          store_row_split(opa_hi, opa_lo, t, f);
-          tph[(j & 1) * kTcTT + t] = B + sgn * Iq * T2;  // the rotation, incl. the Iq T2 term
-          tsc[(j & 1) * kTcTT + t] = Iq * iak;           // 1 / Qt
+        if (has_t) {
+          store_row_split(opa_hi, opa_lo, tid, f);
+          tph[(j & 1) * kTcTT + tid] = tph_v;
+          tsc[(j & 1) * kTcTT + tid] = tsc_v;
         }
       }
       ptx::fence_proxy_async_smem();
