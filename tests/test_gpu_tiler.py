@@ -149,6 +149,8 @@ def _point_sets():
     yield "duplicated points", np.concatenate([dup, dup, dup, dup])[:15000]
     yield "wide strip", np.column_stack([rng.uniform(-8e-3, 8e-3, 24000),
                                          rng.uniform(-2e-4, 2e-4, 24000), np.full(24000, 0.2)])
+    yield "8193 points (a one-point super tile)", grid(91, 10e-6, 0.3)[:8193]
+    yield "10000 identical points", np.tile([[1e-4, -2e-4, 0.3]], (10000, 1))
 
 
 @pytest.mark.parametrize("name,pts", list(_point_sets()), ids=lambda x: x if isinstance(x, str) else "")
