@@ -324,7 +324,8 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
   }
 
   if (precision == HOLO_SPLIT32) {
-    // sort once; pad sources to a multiple of every source tile size (3072 =
+    // tile order (independent of the tile size, so one order serves every
+    // candidate); pad sources to a multiple of every source tile size (3072 =
     // lcm of 1024 and 768; the others divide 1024)
     p->n_pad = std::max<int>(1, (int)((N + 3071) / 3072)) * 3072;
     holo_plan_s *pp = p.get();
