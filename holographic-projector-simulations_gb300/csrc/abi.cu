@@ -758,7 +758,7 @@ int holo_tile_order(holo_handle h, const double *xyz, size_t n, int tiling, int3
       !t.tmp_b || !dorder)
     return fail(HOLO_ERR_ALLOC, "tiler scratch");
   HOLO_TRY(tile_order(dxyz, (int)n, dorder, t, s, tiling));
-  HOLO_CUDA(cudaMemcpyAsync(order, dorder, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  HOLO_CUDA(cudaMemcpyAsync(order, dorder, n * sizeof(int32_t), cudaMemcpyDefault, s));
   HOLO_CUDA(cudaStreamSynchronize(s));
   return HOLO_OK;
 }

@@ -130,8 +130,8 @@ int holo_plan_error_bound(holo_plan p, double *metres);
 #define HOLO_TILE_HILBERT 0
 #define HOLO_TILE_PACKED 1
 /* Tile order of n points (xyz triples, device or host pointer): order[i] = input
- * index of the i-th point in tile order (order: host pointer, n entries).  No
- * reference counterpart. */
+ * index of the i-th point in tile order (order: n entries, host or device pointer;
+ * the call returns when it is written).  No reference counterpart. */
 int holo_tile_order(holo_handle h, const double *xyz, size_t n, int tiling, int32_t *order,
                     holo_stream_t stream);
 /* The tiling a HOLO_SPLIT32 plan used for its sources and for its targets. */

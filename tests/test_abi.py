@@ -63,6 +63,8 @@ def test_host_side_validation_without_gpu(holo):
         lib.holo_destroy(out)
     assert lib.holo_variant_describe(1, 99, None, None, None, None, None, None) == -1
     assert lib.holo_set_variant(None, 1, 0, 0) == -1
+    assert lib.holo_tile_order(None, None, 0, 0, None, None) == -1
+    assert lib.holo_plan_tiling(None, None, None) == -1
 
 
 def test_cli_help_and_argument_errors(holo):
