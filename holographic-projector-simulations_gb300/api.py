@@ -184,13 +184,13 @@ def _device_of(*bufs: _Buf) -> int:
 
 
 # ---- one-shot transforms ------------------------------------------------------------
-_TILINGS = {N.TILE_HILBERT: "hilbert", N.TILE_PACKED: "packed"}
+_TILINGS = {N.TILE_HILBERT: "hilbert", N.TILE_PACKED: "packed", -1: "none"}
 
 
 def tile_order(points, tiling: str = "hilbert") -> np.ndarray:
     """Tile order of a point set (xyz triples, NumPy or torch): order[i] = input index
     of the i-th point in tile order, by the Hilbert or the packed tiling."""
-    codes = {v: k for k, v in _TILINGS.items()}
+    codes = {v: k for k, v in _TILINGS.items() if k >= 0}
     if tiling not in codes:
         raise ValueError(f"tiling must be one of {sorted(codes)}")
     b = _Buf(points, name="points")
@@ -364,7 +364,8 @@ class Plan:
         return ga, gp
 
     def tiling(self) -> dict:
-        """The tiling of the plan's sources and targets: "hilbert" or "packed"."""
+        """The tiling of the plan's sources and targets: "hilbert" or "packed" ("none"
+        for an FP64 plan, which keeps the caller's order)."""
         ts, tt = ctypes.c_int(), ctypes.c_int()
         N.check(self.h.lib.holo_plan_tiling(self.p, ctypes.byref(ts), ctypes.byref(tt)))
         return {"sources": _TILINGS[ts.value], "targets": _TILINGS[tt.value]}

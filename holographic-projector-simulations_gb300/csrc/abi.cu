@@ -423,6 +423,7 @@ int plan_create_impl(holo_handle h, const double *u, size_t N, const double *v, 
     HOLO_TRY(alloc_plan(p.get(), (void **)&p->pos_s, (size_t)3 * p->n_pad * sizeof(double), s));
     HOLO_TRY(alloc_plan(p.get(), (void **)&p->pos_t, (size_t)3 * std::max<size_t>(M, 1) * sizeof(double), s));
     HOLO_TRY(launch_pack_pos(u, (int)N, p->n_pad, p->pos_s, s));
+    p->tiling_s = p->tiling_t = -1;  // the caller's order
     if (M) HOLO_CUDA(cudaMemcpyAsync(p->pos_t, v, 3 * M * sizeof(double), cudaMemcpyDeviceToDevice, s));
   }
   // keep original-order positions for the adjoint's transposed plan

@@ -153,6 +153,12 @@ int blocks_for(int n) {
 
 }  // namespace
 
+int epilogue_preload() {
+  cudaFuncAttributes a;
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_reduce));
+  return HOLO_OK;
+}
+
 int launch_reduce(const double2 *partial, int splits, int M, const int32_t *order, double2 *y,
                   cudaStream_t s) {
   if (M <= 0) return HOLO_OK;

@@ -202,6 +202,9 @@ int launch_pack_ap(const double *amp, const double *phase, int n, int n_pad, dou
                    cudaStream_t s);
 int launch_pack_pos(const double *pos, int n, int n_pad, double *out, cudaStream_t s);
 int launch_iota(int32_t *order, int n, cudaStream_t s);
+// Load the kernels of the Hilbert tiling, the tile boxes and the gathers (CUDA maps a
+// kernel's code on its first use; callers that must not allocate later call this first).
+int tiler_preload_hilbert();
 int launch_rel_hilo(const double *pos_sorted, int n, int n_out, const double *tiles, int tile,
                     float *out, cudaStream_t s);
 int launch_gather_apf(const double *amp, const double *phase, const int32_t *order, int n,
@@ -230,6 +233,7 @@ int launch_fp64(const Fp64Problem &p, int variant, int grid, bool const_phase, i
 int fp64_occupancy(int variant, int *ctas_per_sm);
 
 // epilogue.cu
+int epilogue_preload();  // as tiler_preload_hilbert, for the split reduction
 int launch_reduce(const double2 *partial, int splits, int M, const int32_t *order,
                   double2 *y, cudaStream_t s);
 int launch_reduce_batched(const SplitProblem *probs_dev, const int *prob_offsets, int n_probs,

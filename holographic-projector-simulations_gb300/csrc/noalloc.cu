@@ -44,13 +44,17 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 std::mutex g_noalloc_mu;
 void *g_noalloc_addr[kMaxDevices] = {};
 
-// Device address of the array on `device` (looked up once per device).
+int noalloc_preload();
+
+// Device address of the array on `device` (looked up once per device, which also
+// loads every kernel of the path).
 int noalloc_scratch(int device, unsigned char **out) {
   if (device < 0 || device >= kMaxDevices) return fail(HOLO_ERR_INVALID, "device %d out of range", device);
   if (!g_noalloc_addr[device]) {
     void *ptr = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)", __FILE__, __LINE__);
+    HOLO_TRY(noalloc_preload());
     g_noalloc_addr[device] = ptr;
   }
   *out = static_cast<unsigned char *>(g_noalloc_addr[device]);
@@ -89,6 +93,22 @@ __global__ void __launch_bounds__(256) k_tile_stats(const double *__restrict__ t
     }
   }
 }
+
+// Every kernel this path can launch, loaded now: CUDA maps a kernel's code into
+// device memory on its first use, which a later call must not do.
+int noalloc_preload() {
+  HOLO_TRY(tiler_preload_hilbert());
+  HOLO_TRY(epilogue_preload());
+  cudaFuncAttributes a;
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_tile_stats));
+  for (const size_t m : {(size_t)1, (size_t)1 << 20})  // both preference lists
+    for (const int v : split_preferences(1, m)) {
+      int occ = 0;
+      HOLO_TRY(split_occupancy(v, false, &occ));  // sets the kernel up (and loads it)
+    }
+  return HOLO_OK;
+}
+
 
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 

@@ -716,6 +716,23 @@ int launch_gather_apf(const double *amp, const double *phase, const int32_t *ord
   return HOLO_OK;
 }
 
+int tiler_preload_hilbert() {
+  cudaFuncAttributes a;
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_bbox_partial));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_bbox_final));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_cell_keys));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_hist));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_scan_blocks));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_scan_sums));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_scan_add));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_scatter));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_gather_pos));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_tile_bbox));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_rel_hilo));
+  HOLO_CUDA(cudaFuncGetAttributes(&a, k_gather_apf));
+  return HOLO_OK;
+}
+
 int launch_iota(int32_t *order, int n, cudaStream_t s) {
   if (n <= 0) return HOLO_OK;
   k_iota<<<grid_for(n, 256, 8192), 256, 0, s>>>(order, n); note_launches(1);

@@ -134,7 +134,8 @@ int holo_plan_error_bound(holo_plan p, double *metres);
  * the call returns when it is written).  No reference counterpart. */
 int holo_tile_order(holo_handle h, const double *xyz, size_t n, int tiling, int32_t *order,
                     holo_stream_t stream);
-/* The tiling a HOLO_SPLIT32 plan used for its sources and for its targets. */
+/* The tiling a HOLO_SPLIT32 plan used for its sources and for its targets (-1 for a
+ * HOLO_FP64 plan, which keeps the caller's order). */
 int holo_plan_tiling(holo_plan p, int *tiling_sources, int *tiling_targets);
 
 /* ---- Monte Carlo estimator (transform(), README.md:127; not in the snapshot)

@@ -190,3 +190,5 @@ def test_planner_retiles_where_hilbert_tiles_fail(holo):
     with holo.Plan(grid(64, 10e-6, 0.35), grid(256, 7.56e-6, 0.0), "split32") as pl:
         assert pl.tiling() == {"sources": "hilbert", "targets": "hilbert"}
         assert pl.info()["variant"] == 34
+    with holo.Plan(grid(64, 10e-6, 0.35), grid(64, 7.56e-6, 0.0), "fp64") as pl:
+        assert pl.tiling() == {"sources": "none", "targets": "none"}
