@@ -12,7 +12,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import grid
+from conftest import LAM, grid, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -174,7 +174,7 @@ def test_packed_tiles_are_compact(holo):
         assert worst <= lim * side, (cs, worst / side)
 
 
-def test_planner_retiles_where_hilbert_tiles_fail(holo):
+def test_planner_retiles_where_hilbert_tiles_fail(holo, orc):
     """15838 sources 0.355 m above a 128^2 grid: on Hilbert tiles the bound rules out the
     1024-source tensor-core build (it takes the 512-source one), on packed tiles it holds,
     so the plan keeps the packed tiling and the faster build.  Config 1's planes keep
@@ -187,6 +187,16 @@ def test_planner_retiles_where_hilbert_tiles_fail(holo):
     assert tiling == {"sources": "packed", "targets": "packed"}, tiling
     assert info["variant"] == 34 and info["path_error_bound_m"] <= 3.2e-13, info
     np.testing.assert_array_equal(order, model_order(u))
+    # and the transform on those tiles meets the split path's tolerance
+    rng = np.random.default_rng(5)
+    amp, phase = rng.uniform(0, 1, len(u)), rng.uniform(0, 2 * np.pi, len(u))
+    idx = np.arange(0, len(v), 41)
+    for sign in (-1, 1):
+        with holo.Plan(u, v, "split32") as pl:
+            y = pl.execute(amp, phase, sign, LAM)
+        y = y.cpu().numpy() if hasattr(y, "cpu") else np.asarray(y)
+        ref = orc.transform_subset(amp, phase, u, v, idx, sign, LAM)
+        assert rel_l2(y[idx], ref) < 1e-5, sign
     with holo.Plan(grid(64, 10e-6, 0.35), grid(256, 7.56e-6, 0.0), "split32") as pl:
         assert pl.tiling() == {"sources": "hilbert", "targets": "hilbert"}
         assert pl.info()["variant"] == 34
