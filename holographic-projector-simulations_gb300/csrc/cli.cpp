@@ -20,7 +20,6 @@
 // Exit codes: 0 success; 2 bad arguments or files; 4 non-finite output (the
 // reference's check_complex exit, cuda/util.h:54-60); 3 a library error.
 #include <cuda_runtime.h>
-#include <curand.h>
 #include <getopt.h>
 #include <math.h>
 #include <stdio.h>
@@ -31,13 +30,13 @@
 #include <string>
 #include <vector>
 
+#include "gen.h"
 #include "holo.h"
 #include "io.h"
 
 namespace {
 
 constexpr int kNSqrt = 512;  // N_sqrt (cuda/macros.h:8)
-constexpr double kTwoPi = 2 * M_PI;
 
 template <typename T>
 struct Range {
@@ -240,103 +239,29 @@ double gerp(Range<double> r, double ratio) {
   return pow(10, (1 - ratio) * log10(a) + ratio * log10(b));
 }
 
-// init::plane (cuda/init.h:89-158): lattice with cell-centred points; -r adds
-// the reference's cuRAND (XORWOW, seed 1235, 1236, ...) jitter.
+// init::plane (cuda/init.h:89-158): lattice of cell-centred points on the device
+// (gen.cu); -r adds the reference's cuRAND (XORWOW, seed 1235, 1236, ...) jitter.
 bool lattice(std::vector<double> &v, const holo_io::Plane &p) {
   static unsigned int seed = 1234;
-  const size_t n = v.size() / 3;
-  for (size_t i = 0; i < n; ++i) v[3 * i + 2] = p.offset[2];
-  const size_t x = (size_t)sqrt(n * p.aspect_ratio), y = n / x;
-  const double height = p.width / p.aspect_ratio, dx = p.width / (double)x,
-               dy = height / (double)y, x_half = (p.width - dx) / 2., y_half = (height - dy) / 2.;
-  const double rel_margin = p.randomize ? 0.05 : 0.0, x_random_range = dx - 0.5 * rel_margin * dx,
-               y_random_range = dy - 0.5 * rel_margin * dy;
-  const size_t n_random = x + y;
-  std::vector<float> random(n_random);
-  curandGenerator_t gen = nullptr;
-  float *d_random = nullptr;
-  if (p.randomize) {
-    seed++;
-    if (curandCreateGenerator(&gen, CURAND_RNG_PSEUDO_XORWOW) != CURAND_STATUS_SUCCESS) return false;
-    curandSetPseudoRandomGeneratorSeed(gen, seed);
-    if (cudaMalloc((void **)&d_random, n_random * sizeof(float)) != cudaSuccess) return false;
-  }
-  for (size_t i = 0; i < x; ++i) {
-    if (p.randomize) {
-      curandGenerateUniform(gen, d_random, n_random);
-      curandGenerateUniform(gen, d_random, n_random * sizeof(float) / 32);
-      cudaMemcpy(random.data(), d_random, n_random * sizeof(float), cudaMemcpyDeviceToHost);
-    }
-    for (size_t j = 0; j < y; ++j) {
-      const size_t k = 3 * (j + i * y);
-      v[k] = i * dx - x_half + p.offset[0];
-      v[k + 1] = j * dy - y_half + p.offset[1];
-      v[k + 2] = p.offset[2];
-      if (p.randomize) {
-        v[k] += x_random_range * (random[j * 2] - 0.5);
-        v[k + 1] += y_random_range * (random[j * 2 + 1] - 0.5);
-      }
-    }
-  }
-  if (p.randomize) {
-    curandDestroyGenerator(gen);
-    cudaFree(d_random);
-  }
-  for (size_t i = x * y; i < n; ++i)
-    for (int d = 0; d < 3; ++d) v[3 * i + d] = v[d];
-  return true;
+  if (p.randomize) seed++;
+  return holo_gen::lattice(v.data(), v.size() / 3, p, seed) == 0;
 }
 
-// init::sparse_plane (cuda/init.h:160-234) for the reference's Shape (cuda/main.h:9):
-// the object's points on a line, a line with geometric spacing, a circle, or a
-// circle around a centre point.  Like the reference, line shapes set x only and the
-// dotted circle leaves point 0 as it was (so y, and that point, keep the values of
-// the previous object plane), then the x/y offset is added to every point.
-
-void object_points(std::vector<double> &u, Shape shape, double width, const double *offset,
+// init::sparse_plane (cuda/init.h:160-234) for the reference's Shape (cuda/main.h:9),
+// on the device (gen.cu): the object's points on a line, a line with geometric
+// spacing, a circle, or a circle around a centre point.  Like the reference, line
+// shapes set x only and the dotted circle leaves point 0 as it was (so y, and that
+// point, keep the values of the previous object plane), then the x/y offset is added
+// to every point.
+bool object_points(std::vector<double> &u, Shape shape, double width, const double *offset,
                    double modulate) {
-  const size_t n = u.size() / 3;
-  for (size_t i = 0; i < n; ++i) u[3 * i + 2] = offset[2];
-  if (n == 1) {
-    u[0] = offset[0];
-    u[1] = offset[1];
-    return;
-  }
-  const double radius = width / 2.0, arbitrary_offset = 0.1125 + modulate * kTwoPi;
-  switch (shape) {
-    case Shape::Line: {
-      const double du = width / (double)(n - 1), half_width = width / 2.0;
-      for (size_t i = 0; i < n; ++i) u[3 * i] = i * du - half_width;
-      break;
-    }
-    case Shape::LogLine: {
-      // geomspace(n, 1, 1 + width) (cuda/algebra.h:55-91): 10^(linspace of the logs)
-      const double a = log10(1.0), b = log10(1.0 + width), delta = (b - a) / (n - 1.0);
-      for (size_t i = 0; i < n; ++i) u[3 * i] = pow(10.0, a + delta * i) - 1 + width / 2.;
-      break;
-    }
-    case Shape::Circle: {
-      const double d_phase = kTwoPi / (double)n;
-      for (size_t i = 0; i < n; ++i) {
-        u[3 * i] = sin(i * d_phase + arbitrary_offset) * radius;
-        u[3 * i + 1] = cos(i * d_phase + arbitrary_offset) * radius;
-      }
-      break;
-    }
-    case Shape::DottedCircle: {
-      const double d_phase = kTwoPi / (double)(n - 1);
-      for (size_t i = 1; i < n; ++i) {
-        u[3 * i] = sin(i * d_phase + arbitrary_offset) * radius;
-        u[3 * i + 1] = cos(i * d_phase + arbitrary_offset) * radius;
-      }
-      break;
-    }
-  }
-  if (offset[0] != 0 || offset[1] != 0)
-    for (size_t i = 0; i < n; ++i) {
-      u[3 * i] += offset[0];
-      u[3 * i + 1] += offset[1];
-    }
+  static_assert((int)Shape::Line == holo_gen::kShapeLine &&
+                    (int)Shape::LogLine == holo_gen::kShapeLogLine &&
+                    (int)Shape::Circle == holo_gen::kShapeCircle &&
+                    (int)Shape::DottedCircle == holo_gen::kShapeDottedCircle,
+                "shape codes");
+  return holo_gen::object_points(u.data(), u.size() / 3, (int)shape, width, offset,
+                                 modulate) == 0;
 }
 
 int lib_fail(const char *what, int rc) {
@@ -540,10 +465,11 @@ int generated_mode(Runner &R, const Params &p) {
     const double obj_off[3] = {lerp(p.off_x, ratio), lerp(p.off_y, ratio), gerp(p.off_z, ratio)};
     holo_io::Plane x_plane{lerp(p.obj_width, ratio), {obj_off[0], obj_off[1], obj_off[2]}, 1.0,
                            false};
-    object_points(u, p.shape, x_plane.width, obj_off, i / (double)p.planes_obj);
+    if (!object_points(u, p.shape, x_plane.width, obj_off, i / (double)p.planes_obj))
+      return lib_fail("object points", -2);
     holo_io::Plane y_plane{lerp(p.projector_width, ratio), {0, 0, 0}, p.aspect_projector,
                            p.randomize};
-    if (!lattice(v, y_plane)) return lib_fail("cuRAND", -2);
+    if (!lattice(v, y_plane)) return lib_fail("projector lattice (CUDA / cuRAND)", -2);
     const std::string xs = std::to_string(i);
     int rc;
     if ((rc = write(xa, xp, u, "x" + xs, "u" + xs, x_plane, 0.0, 0.0, p.out_dir))) return rc;
@@ -566,7 +492,7 @@ int generated_mode(Runner &R, const Params &p) {
                              {obj_off[0] + po[0], obj_off[1] + po[1], obj_off[2] + po[2]},
                              p.aspect_projection,
                              p.randomize};
-      if (!lattice(w, z_plane)) return lib_fail("cuRAND", -2);
+      if (!lattice(w, z_plane)) return lib_fail("projection lattice (CUDA / cuRAND)", -2);
       ws.push_back(w);
       zpl.push_back(z_plane);
     }

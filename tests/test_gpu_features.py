@@ -262,6 +262,43 @@ def test_cli_generated_mode(holo, tmp_path):
         assert zf.size == 1024 and np.max(np.abs(zf - za)) < 1e-4
 
 
+def test_cli_generated_lattices(holo, tmp_path):
+    """The projector lattice of the generated-data mode, built on the device
+    (cuda/init.h:89-158): cell centres of a 64 x 64 grid over the 3.584 mm default width
+    exactly; with -r the reference's cuRAND jitter keeps every point within its cell's
+    random range, and two runs agree bit for bit; an aspect ratio below 1 (where the
+    reference reads past its random numbers) runs too."""
+    def run(out, *extra):
+        r = subprocess.run([_cli(holo), "-x", "4", "-y", "4096", "-z", "256", *extra,
+                            "--out", str(out), "--precision", "split32"],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        return holo.io.read_dat(str(out / "v0.dat")).reshape(-1, 3)
+
+    (tmp_path / "a").mkdir()
+    v = run(tmp_path / "a")
+    x = y = 64
+    width = 512 * 7e-6  # the projector's default width (N_sqrt pixels of 7 um)
+    dx = width / x
+    i, j = np.divmod(np.arange(x * y), y)
+    cx = i * dx - (width - dx) / 2
+    cy = j * dx - (width - dx) / 2
+    assert np.allclose(v[:, 0], cx, rtol=0, atol=1e-15) and np.allclose(v[:, 1], cy, rtol=0,
+                                                                        atol=1e-15)
+    assert np.all(v[:, 2] == 0.0)
+    for name in ("b", "c"):
+        (tmp_path / name).mkdir()
+    vb, vc = run(tmp_path / "b", "-r"), run(tmp_path / "c", "-r")
+    assert np.array_equal(vb, vc)
+    half = 0.5 * (dx - 0.5 * 0.05 * dx)
+    assert np.all(np.abs(vb[:, 0] - cx) <= half + 1e-15)
+    assert np.all(np.abs(vb[:, 1] - cy) <= half + 1e-15)
+    assert np.mean(np.abs(vb[:, 0] - cx)) > 0.1 * half  # jittered, not the centres
+    (tmp_path / "d").mkdir()
+    vd = run(tmp_path / "d", "-r", "-a", "0.5")
+    assert np.all(np.isfinite(vd))
+
+
 def test_batched_short_source_tile_groups(holo, orc):
     """Closer planes need narrower tile pairs: 10 um sources 0.2-0.35 m above a 128^2 grid of
     7.56 um select the tensor-core builds with 256- and 512-source tiles and the 1024-source
