@@ -26,11 +26,13 @@
 // pairs of this one are summed: FP64 is slow on this part (a frame is ~6000
 // cycles of dependent FP64 work), so a frame built in the MMA warp held back
 // the first MMA of every tile.  Per pair on the CUDA cores: 3 FP32-pipe ops +
-// 2 MUFU ops.
+// 2 MUFU ops.  Per tile pair the consumers build the operands (each thread its
+// target row and source rows in one straight-line block), then carry the previous
+// tile's sums (float-float, per target) while the first MMAs run.
 //
 // Tiles: 512 targets per CTA (4 blocks of 128), NBLK blocks of 256 sources per
 // tile (1024, 512 or 256 sources; 768 in blocks of 192 with 24 consumer warps);
-// one CTA per SM (up to 213 KB of shared memory).  Shorter source tiles narrow
+// one CTA per SM (up to 217 KB of shared memory).  Shorter source tiles narrow
 // the tile pairs, which tightens the error bound of the first-order model for
 // close or wide point sets, at more per-tile work per pair.  Every wait is bounded:
 // after a timeout the kernel raises the device error word and skips the rest
