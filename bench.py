@@ -136,6 +136,23 @@ def dist_env():
     return rank, world, local
 
 
+def slowest_rank_seconds(local_seconds: float, world: int, device=None) -> float:
+    """The whole job's time over `world` replicas: the slowest rank's (MAX all-reduce;
+    the process group must be up when world > 1)."""
+    if world <= 1:
+        return local_seconds
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([local_seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt)
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units all `world` replicas processed, per second of the slowest rank."""
+    return world * units_per_rank / seconds
+
+
 def cpu_baseline(amp, phase, u, v, seconds: float = 12.0) -> dict:
     """The C oracle (FP64, every host thread) on a bounded sample of y-pass targets."""
     import oracle
@@ -476,12 +493,8 @@ def main():
     launches = api.kernel_launches() - launches0
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_s = sum(step_ms) * 1e-3
-    if world > 1:
-        tt = torch.tensor([total_s], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_s = float(tt)
-    value = world * pairs_step * args.steps / total_s
+    total_s = slowest_rank_seconds(sum(step_ms) * 1e-3, world, dev)
+    value = whole_job_rate(pairs_step * args.steps, world, total_s)
 
     # e2e: the C ABI with host buffers, copies inside the timing
     e2e_steps = max(1, min(args.steps, 3))
@@ -491,7 +504,7 @@ def main():
     for _ in range(e2e_steps):
         holo.project(amp, phase, u, v, w, LAM, precision=args.precision)
     barrier()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = slowest_rank_seconds((time.perf_counter() - t0) / e2e_steps, world, dev)
     h2d = 8 * (2 * N + 3 * N + 3 * M + 3 * P)
     d2h = 8 * (2 * M + 2 * P)
 
@@ -575,7 +588,7 @@ def main():
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "roofline": roofline,
         "cpu_baseline": cpu,
-        "e2e": {"value": world * pairs_step / e2e_s, "unit": "pair-evals/s",
+        "e2e": {"value": whole_job_rate(pairs_step, world, e2e_s), "unit": "pair-evals/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * e2e_s},
         "gpu_launches": launches,
