@@ -551,6 +551,24 @@ def main():
                 "kernel_pairs_per_s": kern_pairs_s,
                 "kernel_ms_per_launch": kern_ms / max(kern_launches, 1),
                 "kernel_launches": kern_launches}
+    # the same kernel against the measured copy bandwidth and bf16 GEMM rate: it
+    # moves ~1e-4 bytes per pair and runs 4 TF32 MMAs of K = 8 per pair (64 FLOP; TF32
+    # issues at half the bf16 rate), far from both
+    peaks_path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path) and kern_launches and var and var.get("pair_loop") == 3:
+        peaks = json.load(open(peaks_path))
+        launch_s = kern_ms * 1e-3 / kern_launches
+        tc_tflops = 64.0 * kern_pairs_s / 1e12
+        roofline["measured_peaks"] = {
+            "source": "MEASURED_PEAKS.json (copy bandwidth; cuBLAS bf16 burst)",
+            "hbm_gbs": peaks.get("hbm_gbs"),
+            "dram_gbs": traffic / launch_s / 1e9 if traffic else None,
+            "hbm_frac": traffic / launch_s / 1e9 / peaks["hbm_gbs"]
+            if traffic and peaks.get("hbm_gbs") else None,
+            "bf16_tflops": peaks.get("bf16_tflops"),
+            "tf32_mma_tflops": tc_tflops,
+            "tensor_frac_of_bf16": tc_tflops / peaks["bf16_tflops"]
+            if peaks.get("bf16_tflops") else None}
 
     # split-FP32 vs the plain FP64 kernel on a bounded target subset
     rng = np.random.default_rng(1)
