@@ -85,19 +85,19 @@ struct TcSmem {
   static constexpr size_t opa_hi = opb_a + kTcCS * kTcK * 4;           // float [TT*8]
   static constexpr size_t opa_lo = opa_hi + kTcTT * kTcK * 4;          // float [TT*8]
   static constexpr size_t opa_one = opa_lo + kTcTT * kTcK * 4;         // float [128*8]: (1,1,1,0..)
-  static constexpr size_t amp = opa_one + kTcM * kTcK * 4;             // float [CS]
+  static constexpr size_t amp = opa_one + kTcM * kTcK * 4;             // float [2][CS]
   // partial sums, [PB][CG][TT] float2: a tile's are carried during the next tile, and
   // with fewer than three source blocks per tile a consumer can write the next
   // tile's before a slower one has carried them, so those builds keep two buffers
   static constexpr int PB = NBLK >= 3 ? 1 : 2;
-  static constexpr size_t part = amp + kTcCS * 4;
+  static constexpr size_t part = amp + 2 * kTcCS * 4;
   static constexpr size_t acc = part + PB * CG * kTcTT * 8;            // float4 [TT]
   static constexpr size_t tph = acc + kTcTT * 16;                      // float [2][TT]
   static constexpr size_t tsc = tph + 2 * kTcTT * 4;                   // float [2][TT]
   static constexpr size_t tgeo = tsc + 2 * kTcTT * 4;                  // float [6][TT]
   static constexpr size_t frame = tgeo + 6 * kTcTT * 4;                // Frame [2]
-  static constexpr size_t bars = (frame + 2 * sizeof(Frame) + 15) / 16 * 16;  // uint64 [5]
-  static constexpr size_t misc = bars + 5 * 8;                         // uint32 taddr, abort
+  static constexpr size_t bars = (frame + 2 * sizeof(Frame) + 15) / 16 * 16;  // uint64 [6]
+  static constexpr size_t misc = bars + 6 * 8;                         // uint32 taddr, abort
   static constexpr size_t bytes = misc + 16;
 };
 template <int CG, int NBLK>
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
   float *tgeo = reinterpret_cast<float *>(smem + L::tgeo);  // this item's target records
   Frame *frames = reinterpret_cast<Frame *>(smem + L::frame);  // tile j in frames[j & 1]
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bars);
-  uint64_t *bar_tma = bars, *full = bars + 1, *freeb = bars + 3;
+  uint64_t *bar_tma = bars, *full = bars + 1, *freeb = bars + 3, *frame_ready = bars + 5;
   uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(smem + L::misc);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + L::misc + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -188,6 +188,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
     ptx::mbar_init(&full[1], 1);
     ptx::mbar_init(&freeb[0], kTcConsumers);
     ptx::mbar_init(&freeb[1], kTcConsumers);
+    ptx::mbar_init(frame_ready, 1);
     *abort_flag = 0;
     ptx::fence_barrier_init();
   }
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
   const uint32_t tbase = *taddr_slot;
 
   constexpr uint32_t idesc = ptx::tc_idesc_tf32(kTcM, kTcN);
-  uint32_t par_tma = 0;
+  uint32_t par_tma = 0, n_frames = 0;
   // producer: MMA groups issued per TMEM buffer; consumers: completions consumed
   uint32_t uses[2] = {0u, 0u};
   __shared__ int s_item;
@@ -278,11 +279,31 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
       Frame *fr = frames + (j & 1);
       // the first tile's frame here; the next ones by the frame warp during the
       // previous tile's pair work
-      if (framer && lane == 0 && j == sb)
+      if (framer && lane == 0 && j == sb) {
         build_frame(fr, P.tiles_t + 6 * (size_t)tt, P.tiles_s + 6 * (size_t)j, sk);
-      tc_wait(bar_tma, par_tma, abort_flag, err);
+        ptx::mbar_arrive(frame_ready);
+      }
+      // With kOverlapTiles there is no block-wide barrier here after an item's first
+      // tile: consumers done with the previous tile build this one's operands while
+      // slower ones finish it.  What the barrier orders is then ordered per consumer:
+      // the staged records by the bulk copy's barrier, the frame by frame_ready, the
+      // amplitudes by their second buffer; the operand tiles are read only by MMAs of
+      // the previous tile, all complete once this consumer saw its last block, and
+      // each thread writes and carries only its own target's rotation.  Measured on
+      // one GB300 (each build against itself, two runs, 0.02 % apart): the overlap
+      // is 0.8 % faster for single problems with 1024- and 256-source tiles, 0.85 %
+      // slower with 512-source tiles, and 1.25 % faster for a batch of 64 uneven
+      // problems than a work queue that keeps the barrier for its 2-block builds.
+      constexpr bool kOverlapTiles = BATCHED || NBLK != 2;
+      if (j == sb || !kOverlapTiles) {
+        tc_wait(bar_tma, par_tma, abort_flag, err);
+        __syncthreads();  // frame and staged records visible (and, first tile, the rest)
+      } else if (consumer) {
+        tc_wait(bar_tma, par_tma, abort_flag, err);
+      }
       par_tma ^= 1u;
-      __syncthreads();  // frame and staged records visible
+      if (kOverlapTiles && consumer) tc_wait(frame_ready, n_frames & 1u, abort_flag, err);
+      ++n_frames;
 
       // ---- operands of this tile pair (consumer threads) ----
       if (consumer && !*abort_flag) {
@@ -364,7 +385,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
           *reinterpret_cast<float4 *>(opb_a + tc_off(i, 0)) =
               make_float4(a3[r][0], a3[r][1], a3[r][2], 0.f);
           *reinterpret_cast<float4 *>(opb_a + tc_off(i, 4)) = z;
-          amp[i] = am[r];
+          amp[(j & 1) * kTcCS + i] = am[r];
         }
         if (has_t) {
           store_row_split(opa_hi, opa_lo, tid, f);
@@ -379,10 +400,13 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
       if (tid == 0 && j + 1 < se && !*abort_flag) issue(j + 1);
 
       if (framer) {
-        // frames[(j + 1) & 1] was last read by the operand build of tile j - 1
-        if (lane == 0 && j + 1 < se)
+        // frames[(j + 1) & 1] was last read by the operand build of tile j - 1, and it
+        // is read next after frame_ready's next phase: it runs at most one phase ahead
+        if (lane == 0 && j + 1 < se) {
           build_frame(frames + ((j + 1) & 1), P.tiles_t + 6 * (size_t)tt,
                       P.tiles_s + 6 * (size_t)(j + 1), sk);
+          ptx::mbar_arrive(frame_ready);
+        }
         __syncwarp();
       } else if (producer) {
         // ---- MMA issue: 4 target blocks x NBLK source blocks, double-buffered ----
@@ -438,7 +462,8 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
                 if (ch + 1 < S::Chunks)
                   ptx::tmem_ld16_nowait(ta + (uint32_t)(16 * (ch + 1)), rv[(ch + 1) & 1]);
                 const float4 *ap =
-                    reinterpret_cast<const float4 *>(amp + n * kTcN + cg * S::Cols + 16 * ch);
+                    reinterpret_cast<const float4 *>(amp + (j & 1) * kTcCS + n * kTcN +
+                                                     cg * S::Cols + 16 * ch);
                 float av[16];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
