@@ -39,18 +39,21 @@ FLOP_PER_PAIR = 29   # the reference's FLOP_PER_POINT (cuda/macros.h:71-80)
 def pipe_ops_per_pair(variant: dict) -> tuple[float, float]:
     """(MUFU ops, FP32-pipe ops) per pair of a split-kernel variant, by pair model:
     0 (curvature correction): 3 MUFU (rsqrt, sin, cos) + 12 FP32; 1 (without it):
-    3 + 10; 2 (1/q series, no rsqrt): 2 + 8; 3 (phase from tensor-core MMAs): 2 + 3.  `fma_sincos_targets` of every
-    `targets_per_thread` take sin/cos from the FMA-pipe polynomial instead
-    (+16 FP32, -2 MUFU); with warp-specialised sin/cos (pair loop 2) a quarter of the
-    warps do."""
+    3 + 10; 2 (1/q series, no rsqrt): 2 + 8; 3 (phase from tensor-core MMAs): 2 + 3.
+    `fma_sincos_targets` of every `targets_per_thread` take sin/cos from the FMA-pipe
+    polynomial instead (-2 MUFU; +16 FP32 for the full-turn form of the CUDA-core loops,
+    +13 for the half-turn form of the tensor-core kernel); with warp-specialised sin/cos
+    (pair loop 2) a quarter of the warps do."""
     f = variant["fma_sincos_targets"] / variant["targets_per_thread"]
     if variant.get("pair_loop", 0) == 2:
         f = 0.25
+    poly = 16.0
     if variant.get("pair_loop", 0) == 3:  # tensor-core phase: `fma_sincos_targets` of 16 pairs
         f = variant["fma_sincos_targets"] / 16.0
+        poly = 13.0
     mufu, fp32 = {0: (3.0, 12.0), 1: (3.0, 10.0), 2: (2.0, 8.0),
                   3: (2.0, 3.0)}[variant.get("pair_model", 0)]
-    return mufu - 2.0 * f, fp32 + 16.0 * f
+    return mufu - 2.0 * f, fp32 + poly * f
 
 
 WORKLOAD = "config2: 512^2 sources -> 1024^2 projector -> 512^2 projection (x->y->z)"
@@ -570,7 +573,8 @@ def main():
             "tensor_frac_of_bf16": tc_tflops / peaks["bf16_tflops"]
             if peaks.get("bf16_tflops") else None}
 
-    # split-FP32 vs the plain FP64 kernel on a bounded target subset
+    # split-FP32 vs the plain FP64 kernel on a bounded target subset; the split result
+    # is the full y pass (the timed tiling and variant) read at those targets
     rng = np.random.default_rng(1)
     idx = np.sort(rng.choice(M, 8192, replace=False))
     d_vs = t(v[idx])
@@ -582,7 +586,9 @@ def main():
     e1.record()
     barrier()
     fp64_rate = N * len(idx) / (e0.elapsed_time(e1) * 1e-3)
-    y32 = holo.transform(d_amp, d_phase, d_u, d_vs, -1, LAM, precision="split32")
+    with holo.Plan(d_u, d_v, args.precision) as pl:
+        y32 = pl.execute(d_amp, d_phase, -1, LAM)[torch.as_tensor(idx, device=dev)]
+        acc_variant = pl.info()["variant"]
     torch.cuda.synchronize()
     a32, a64 = y32.cpu().numpy(), y64.cpu().numpy()
     rel = float(np.linalg.norm(a32 - a64) / np.linalg.norm(a64))
@@ -614,6 +620,8 @@ def main():
         "fp64_kernel_pairs_per_s": fp64_rate,
         "split_over_fp64": kern_pairs_s / fp64_rate if fp64_rate else None,
         "rel_l2_split_vs_fp64": rel, "max_phase_err_rad": phase_err,
+        "accuracy_check": {"targets": len(idx), "variant": acc_variant,
+                           "precision": args.precision},
         "flops_29_per_pair": value * FLOP_PER_PAIR,
         "wall_s_timed": wall,
         "published_reference_pairs_per_s": {"value": 5.3e10, "what": "reference kernel #2, "

@@ -488,10 +488,12 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
                     continue;
                   }
                   const uint64_t t2 = ptx::pack2(t0, t1);
-                  const uint64_t am = ptx::pack2(av[2 * pp], av[2 * pp + 1]);
+                  uint64_t am = ptx::pack2(av[2 * pp], av[2 * pp + 1]);
                   uint64_t sn, cs;
                   if (pp < npp) {
-                    poly_sincos2(t2, sn, cs);  // FMA pipe
+                    uint64_t sign;
+                    poly_sincos2_half(t2, sn, cs, sign);  // FMA pipe
+                    am ^= sign;
                   } else {
                     sn = ptx::pack2(ptx::sin_approx(t0), ptx::sin_approx(t1));  // XU pipe
                     cs = ptx::pack2(ptx::cos_approx(t0), ptx::cos_approx(t1));

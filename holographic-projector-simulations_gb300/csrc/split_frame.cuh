@@ -124,6 +124,36 @@ __device__ __forceinline__ uint64_t splat2(float k) {
   return (b << 32) | b;
 }
 
+// sin and cos of a packed pair of angles reduced to half turns: th = pi (n + g),
+// n = rint(th / pi), |g| <= 1/2.  sin(pi g) = g P(g^2) (degree 9) and cos(pi g) =
+// Q(g^2) (degree 8), minimax fits on |g| <= 1/2 made by gen_sincos_poly.py (float32
+// Horner error 2.0e-7 and 1.9e-7, against 7.5e-7 and 4.2e-7 for poly_sincos2); beyond
+// |th| = pi the rounding of th / pi dominates, as for any FP32 reduction.  The (-1)^n
+// that both share is returned as a sign mask (bit 31 of each half) for the caller to
+// put on the amplitude: 14 packed FP32 instructions per two angles against 17 for
+// poly_sincos2, plus two integer ones per half for the sign.  Measured on one GB300:
+// the tensor-core kernel 1.6 % faster at 6 of 16 source pairs; in packed_pairs, where
+// each of a thread's targets needs its own flip of the shared amplitudes, 1.1-1.3 %
+// slower for 1024-source tiles (2.4 % faster for 256), so packed_pairs keeps poly_sincos2.
+__device__ __forceinline__ void poly_sincos2_half(uint64_t th, uint64_t &sn, uint64_t &cs,
+                                                  uint64_t &sign) {
+  const uint64_t h = ptx::mul2(th, splat2(3.183098733e-01f));
+  const uint64_t u = ptx::add2(h, splat2(12582912.0f));  // rint(h) in the low bits
+  const uint64_t g = ptx::sub2(h, ptx::sub2(u, splat2(12582912.0f)));
+  const uint64_t g2 = ptx::mul2(g, g);
+  uint64_t s = ptx::fma2(splat2(7.722012699e-02f), g2, splat2(-5.980451703e-01f));
+  s = ptx::fma2(s, g2, splat2(2.550031424e+00f));
+  s = ptx::fma2(s, g2, splat2(-5.167706966e+00f));
+  s = ptx::fma2(s, g2, splat2(3.141592503e+00f));
+  uint64_t c = ptx::fma2(splat2(2.196968049e-01f), g2, splat2(-1.331880212e+00f));
+  c = ptx::fma2(c, g2, splat2(4.058412075e+00f));
+  c = ptx::fma2(c, g2, splat2(-4.934792995e+00f));
+  c = ptx::fma2(c, g2, splat2(9.999999404e-01f));
+  sn = ptx::mul2(s, g);
+  cs = c;
+  sign = (u << 31) & 0x8000000080000000ull;  // bit 0 of each half: n odd
+}
+
 // poly_sincos on a packed pair of angles (fma.rn.f32x2 and friends): the same
 // polynomial and operation order as poly_sincos, two angles per instruction.
 __device__ __forceinline__ void poly_sincos2(uint64_t th, uint64_t &sn, uint64_t &cs) {
