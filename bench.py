@@ -56,7 +56,7 @@ def pipe_ops_per_pair(variant: dict) -> tuple[float, float]:
     return mufu - 2.0 * f, fp32 + poly * f
 
 
-WORKLOAD = "config2: 512^2 sources -> 1024^2 projector -> 512^2 projection (x->y->z)"
+WORKLOAD = "chain512: 512^2 sources -> 1024^2 projector -> 512^2 projection (x->y->z)"
 
 
 def grid(n, pitch, z):
@@ -280,7 +280,8 @@ def _events_ms(fn, reps=1):
 
 
 def run_other_workload(args):
-    """Configs 1, 3, 4, 5: one JSON line each (not the headline line)."""
+    """The chain64, mc16, batch64 and adam1024 workloads: one JSON line each (not the
+    headline line)."""
     import torch
     import __graft_entry__ as entry
     entry._load_build_module().build()
@@ -294,13 +295,13 @@ def run_other_workload(args):
         return grid(n, pitch, z)
 
     out = {"workload": args.workload, "data": "synthetic (seeded)"}
-    if args.workload in ("config1", "config3"):
+    if args.workload in ("chain64", "mc16"):
         u = grid(64, 10e-6, 0.35)
         v = grid(256, 7.56e-6, 0.0)
         amp = rng.uniform(0, 1, len(u))
         phase = rng.uniform(0, 2 * np.pi, len(u))
         d = [t(a) for a in (amp, phase, u, v, u)]
-        if args.workload == "config1":
+        if args.workload == "chain64":
             for prec in ("fp64", "split32"):
                 holo.project(*d, LAM, precision=prec)
                 ms, _ = _events_ms(lambda: holo.project(*d, LAM, precision=prec), reps=3)
@@ -322,8 +323,9 @@ def run_other_workload(args):
                 "effective_pair_evals_per_s": len(u) * len(v) / (ms * 1e-3),
                 "mc_rel_l2_vs_fp64": float(np.linalg.norm(ymc - y64) / np.linalg.norm(y64)),
                 "mc_expected_rel_l2": mc_expected_rel_l2(amp, u, v, y64, 16),
-                "config": "x->y pass of config 1, 1/16 of the sources per block of 256 targets"})
-    elif args.workload == "config4":
+                "config": "x->y pass of the 64^2 -> 256^2 chain, 1/16 of the sources per block of "
+                          "256 targets"})
+    elif args.workload == "batch64":
         probs, pairs = [], 0
         for i in range(64):
             ns = int(np.exp(rng.uniform(np.log(1024), np.log(262144))))
@@ -350,7 +352,7 @@ def run_other_workload(args):
                     "sequential_pair_evals_per_s": pairs / (ms_s * 1e-3),
                     "speedup": ms_s / ms_b,
                     "config": "N log-uniform [1024, 262144], M in {128^2..1024^2}, z0 U[0.2,0.5]"})
-    else:  # config5
+    else:  # adam1024
         pp = t(grid(1024, 7.56e-6, 0.0)).reshape(-1, 3)
         tp = t(grid(512, 10e-6, 0.35)).reshape(-1, 3)
         n = 512
@@ -429,9 +431,9 @@ def main():
                          "(--profile-case: the first one is forced)")
     ap.add_argument("--sweep-variants", action="store_true",
                     help="time every split-FP32 kernel variant on the config-2 y pass, then exit")
-    ap.add_argument("--workload", default="config2",
-                    choices=["config2", "config1", "config3", "config4", "config5"],
-                    help="config2 (default) is the headline line; the others print their own "
+    ap.add_argument("--workload", default="chain512",
+                    choices=["chain512", "chain64", "mc16", "batch64", "adam1024"],
+                    help="chain512 (default) is the headline line; the others print their own "
                          "JSON line: 1 FP64 chain, 3 Monte Carlo, 4 batched, 5 Adam hologram")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -440,7 +442,7 @@ def main():
         return run_profile_case(args)
     if args.sweep_variants:
         return run_sweep(args)
-    if args.workload != "config2":
+    if args.workload != "chain512":
         return run_other_workload(args)
 
     import torch
@@ -523,7 +525,7 @@ def main():
     achieved = kern_pairs_s * MUFU_PER_PAIR
     # DRAM bytes per pair-kernel launch (the y pass) from the committed ncu capture
     traffic = None
-    prof = os.path.join(REPO, "profiles", "k_split_traffic_config2.md")
+    prof = os.path.join(REPO, "profiles", "k_split_traffic_chain512.md")
     if os.path.exists(prof) and args.precision == "split32":
         for line in open(prof):
             if line.startswith("bytes_per_launch_y_pass:"):

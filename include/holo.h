@@ -158,7 +158,7 @@ int holo_plan_execute_mc(holo_plan p, int sign, double lambda, const double *amp
  * conjugate-transposed sum w_n = e^{i phi_n} conj(sum_m G_m e^{-i s k r}/r) and
  * writes grad_amp[n] = Re w_n, grad_phase[n] = -a_n Im w_n.  The N x M phasor
  * matrix is never stored.  (No reference counterpart: the reference has no
- * gradients; BASELINE config 5.) */
+ * gradients; e.g. 1024^2 projector phases against a 512^2 target.) */
 int holo_plan_adjoint(holo_plan p, int sign, double lambda, const double *amp,
                       const double *phase, const double *grad_y, double *grad_amp,
                       double *grad_phase, holo_stream_t stream);

@@ -64,7 +64,7 @@ def grid(n: int, pitch: float, z: float, ny: int | None = None) -> np.ndarray:
     return np.stack([X.ravel(), Y.ravel(), np.full(n * ny, z)], axis=1)
 
 
-def config1(seed: int = 0):
+def chain64(seed: int = 0):
     """64x64 source grid (10 um, z = 0.35 m), 256x256 projector (7.56 um, z = 0)."""
     rng = np.random.default_rng(seed)
     u = grid(64, 10e-6, 0.35)
@@ -86,7 +86,7 @@ def gaussian_blobs(n: int, rng, count: int = 8) -> np.ndarray:
     return (img / img.max()).ravel()
 
 
-def config2(seed: int = 0):
+def chain512(seed: int = 0):
     """512x512 sources (Gaussian-blob amplitudes), 1024x1024 projector, z = 512x512."""
     rng = np.random.default_rng(seed)
     u = grid(512, 10e-6, 0.35)

@@ -9,15 +9,15 @@ import time
 import numpy as np
 import pytest
 
-from conftest import LAM, config1, grid, rel_l2
+from conftest import LAM, chain64, grid, rel_l2
 
 pytestmark = pytest.mark.gpu
 
 
-# ---- Monte Carlo (config 3) ------------------------------------------------------------
+# ---- Monte Carlo (1/16, 64^2 -> 256^2) --------------------------------------------------
 def test_mc_matches_oracle_restatement(holo, orc):
     """Same strata, blocks and Philox picks as the oracle, given the plan's tile orders."""
-    amp, phase, u, v, _ = config1()
+    amp, phase, u, v, _ = chain64()
     v = v[:16384]
     with holo.Plan(u, v, "split32") as pl:
         so, to = pl.order(0), pl.order(1)
@@ -28,26 +28,26 @@ def test_mc_matches_oracle_restatement(holo, orc):
 
 
 def test_mc_full_sampling_is_brute_force(holo, orc):
-    amp, phase, u, v, _ = config1()
+    amp, phase, u, v, _ = chain64()
     v = v[:8192]
     y = holo.transform_mc(amp, phase, u, v, -1, LAM, seed=1, subsample=1, targets_per_block=256)
     assert rel_l2(y, orc.transform(amp, phase, u, v, -1, LAM)) < 1e-5
 
 
-def test_mc_config3_error_and_unbiasedness(holo, orc):
-    """Config 3: 1/16 of the sources per block of 256 targets, x16 (report rel-L2)."""
-    amp, phase, u, v, _ = config1()
+def test_mc16_error_and_unbiasedness(holo, orc):
+    """64^2 -> 256^2 with 1/16 of the sources per block of 256 targets, x16 (report rel-L2)."""
+    amp, phase, u, v, _ = chain64()
     v = v[:4096]
     ref = orc.transform(amp, phase, u, v, -1, LAM)
     runs = np.array([holo.transform_mc(amp, phase, u, v, -1, LAM, seed=s, subsample=16,
                                        targets_per_block=256) for s in range(64)])
     single = np.mean([rel_l2(r, ref) for r in runs])
     mean_err = rel_l2(runs.mean(0), ref)
-    print(f"config3: MC rel-L2 single {single:.3f}, mean of 64 {mean_err:.3f}")
+    print(f"mc16: MC rel-L2 single {single:.3f}, mean of 64 {mean_err:.3f}")
     assert mean_err < 2.0 * single / math.sqrt(64)
 
 
-# ---- adjoint (config 5) -----------------------------------------------------------------
+# ---- adjoint (phase-only holograms) -----------------------------------------------------
 def _small_problem(seed=0, n=256, m=4096):
     import torch
     rng = np.random.default_rng(seed)
@@ -150,7 +150,7 @@ def test_phase_hologram_optimisation_decreases_loss(holo):
     assert losses[-1] < 0.7 * losses[0]
 
 
-# ---- batched persistent launch (config 4) -------------------------------------------------
+# ---- batched persistent launch (uneven) ---------------------------------------------------
 def test_batched_matches_individual(holo, orc):
     import torch
     dev = torch.device("cuda:0")
@@ -414,7 +414,7 @@ def test_bounded_wait_timeout_is_reported_and_the_context_survives(holo, orc):
     assert b"ran out" in lib.holo_last_error_string()
     assert lib.holo_device_status(h.h, None) == 0  # cleared by the report
     assert lib.holo_selftest_bounded_wait(h.h, 0, None) == holo._native.ERR_INVALID
-    amp, phase, u, v, _ = config1(seed=4)
+    amp, phase, u, v, _ = chain64(seed=4)
     u, amp, phase, v = u[:1024], amp[:1024], phase[:1024], v[:4096]
     for prec, tol in (("fp64", 1e-12), ("split32", 1e-5)):
         y = holo.transform(amp, phase, u, v, -1, LAM, precision=prec)

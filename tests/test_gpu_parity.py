@@ -9,7 +9,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, LAM, config1, config2, grid, max_phase_err, rel_l2
+from conftest import GOLDEN, LAM, chain64, chain512, grid, max_phase_err, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -30,9 +30,9 @@ def test_golden_small_transform(holo, orc, prec):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "split32"])
-def test_config1_chain(holo, orc, prec):
-    """Config 1: 4096 sources -> 65,536 projector pixels -> 4096 projection points."""
-    amp, phase, u, v, w = config1()
+def test_chain64(holo, orc, prec):
+    """64^2 chain: 4096 sources -> 65,536 projector pixels -> 4096 projection points."""
+    amp, phase, u, v, w = chain64()
     y = holo.transform(amp, phase, u, v, -1, LAM, precision=prec)
     y_ref = orc.transform(amp, phase, u, v, -1, LAM)
     assert rel_l2(y, y_ref) < TOL[prec]
@@ -48,7 +48,7 @@ def test_config1_chain(holo, orc, prec):
 @pytest.mark.parametrize("prec", ["fp64", "split32"])
 def test_project_chain_matches_oracle(holo, orc, prec):
     """holo_project: normalised polar y and z (cuda/main.cu:186, 213-216 semantics)."""
-    amp, phase, u, v, w = config1(seed=5)
+    amp, phase, u, v, w = chain64(seed=5)
     u, v, w = u[:1024], v[:16384], w[:2048]
     amp, phase = amp[:1024], phase[:1024]
     ya, yp, za, zp = holo.project(amp, phase, u, v, w, LAM, precision=prec)
@@ -112,7 +112,7 @@ def test_tilted_and_3d_geometry(holo, orc, prec):
 def test_const_phase_counts_sources(holo, prec):
     """TEST_CONST_PHASE (cuda/superposition.cu:113-116): every term 1+0i, so y_m == N exactly,
     through source splits, partial sums and the scatter back to caller order."""
-    amp, phase, u, v, _ = config1()
+    amp, phase, u, v, _ = chain64()
     for n, m in ((4096, 65536), (4096, 300), (1000, 5000)):
         y = holo.transform(amp[:n], phase[:n], u[:n], v[:m], -1, LAM, precision=prec,
                            flags=holo.FLAG_CONST_PHASE)
@@ -121,23 +121,23 @@ def test_const_phase_counts_sources(holo, prec):
 
 @pytest.mark.parametrize("prec", ["fp64", "split32"])
 def test_deterministic(holo, prec):
-    amp, phase, u, v, _ = config1(seed=2)
+    amp, phase, u, v, _ = chain64(seed=2)
     a = holo.transform(amp, phase, u, v[:20000], -1, LAM, precision=prec)
     b = holo.transform(amp, phase, u, v[:20000], -1, LAM, precision=prec)
     assert np.array_equal(a, b)
 
 
-def test_config2_split_vs_fp64_kernel(holo, orc):
-    """Config 2 at full source count: split-FP32 vs the FP64 kernel (validated above against
+def test_chain512_split_vs_fp64_kernel(holo, orc):
+    """512^2 sources -> 1024^2 projector at full source count: split-FP32 vs the FP64 kernel (validated above against
     the CPU oracle) on a seeded 4096-target subset, and vs the CPU oracle on 64 targets."""
     import torch
-    amp, phase, u, v, _ = config2()
+    amp, phase, u, v, _ = chain512()
     rng = np.random.default_rng(1)
     idx = np.sort(rng.choice(len(v), 4096, replace=False))
     ys = holo.transform(amp, phase, u, v[idx], -1, LAM, precision="split32")
     yd = holo.transform(amp, phase, u, v[idx], -1, LAM, precision="fp64")
     err = rel_l2(ys, yd)
-    print(f"config2 subset: rel-L2 {err:.3e}, max phase err {max_phase_err(ys, yd):.3e}")
+    print(f"chain512 subset: rel-L2 {err:.3e}, max phase err {max_phase_err(ys, yd):.3e}")
     assert err < 1e-5
     yc = orc.transform_subset(amp, phase, u, v, idx[:64], -1, LAM)
     assert rel_l2(yd[:64], yc) < 1e-12
@@ -151,7 +151,7 @@ def test_config2_split_vs_fp64_kernel(holo, orc):
 
 
 def test_plan_reuse_and_orders(holo, orc):
-    amp, phase, u, v, _ = config1(seed=3)
+    amp, phase, u, v, _ = chain64(seed=3)
     with holo.Plan(u, v[:30000], "split32") as pl:
         so, to = pl.order(0), pl.order(1)
         assert np.array_equal(np.sort(so), np.arange(len(u)))
@@ -164,7 +164,7 @@ def test_plan_reuse_and_orders(holo, orc):
 
 def test_torch_device_path_is_async_and_matches(holo, orc):
     import torch
-    amp, phase, u, v, _ = config1(seed=4)
+    amp, phase, u, v, _ = chain64(seed=4)
     dev = torch.device("cuda:0")
     t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
     y = holo.transform(t(amp), t(phase), t(u), t(v), -1, LAM, precision="split32")
@@ -175,7 +175,7 @@ def test_torch_device_path_is_async_and_matches(holo, orc):
 
 
 def test_invalid_arguments_return_status(holo):
-    amp, phase, u, v, _ = config1()
+    amp, phase, u, v, _ = chain64()
     with pytest.raises(ValueError):  # the Python layer rejects it first
         holo.transform(amp, phase, u, v, 0, LAM)
     lib, h = holo._native.load(), holo.handle(0)
@@ -196,7 +196,7 @@ def test_invalid_arguments_return_status(holo):
 
 def test_reference_wave_amplitude_only(holo, orc):
     """PROJECT_PHASE=0 path (cuda/transform.cu:379-395) restated with the oracle."""
-    amp, phase, u, v, _ = config1(seed=6)
+    amp, phase, u, v, _ = chain64(seed=6)
     u, amp, phase, v = u[:512], amp[:512], phase[:512], v[:8192]
     ya, yp, _, _ = holo.project(amp, phase, u, v, None, LAM, precision="fp64",
                                 reference_wave=True, reference_distance=0.25)

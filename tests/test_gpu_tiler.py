@@ -177,7 +177,7 @@ def test_packed_tiles_are_compact(holo):
 def test_planner_retiles_where_hilbert_tiles_fail(holo, orc):
     """15838 sources 0.355 m above a 128^2 grid: on Hilbert tiles the bound rules out the
     1024-source tensor-core build (it takes the 512-source one), on packed tiles it holds,
-    so the plan keeps the packed tiling and the faster build.  Config 1's planes keep
+    so the plan keeps the packed tiling and the faster build.  The 64^2 chain's planes keep
     the Hilbert tiles."""
     u = grid(126, 10e-6, 0.355)[:15838]
     v = grid(128, 7.56e-6, 0.0)

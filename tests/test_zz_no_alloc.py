@@ -14,7 +14,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from conftest import LAM, config1, rel_l2
+from conftest import LAM, chain64, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -33,7 +33,7 @@ def test_noalloc_matches_allocating_entry_point(holo):
     T = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
     free = []
     for seed, m, sign in ((0, 65536, -1), (1, 30000, +1)):  # two calls in a row
-        amp, phase, u, v, _ = config1(seed)
+        amp, phase, u, v, _ = chain64(seed)
         v = v[:m]
         ta, tp, tu, tv = T(amp), T(phase), T(u), T(v)
         y = torch.full((2 * m,), float("nan"), dtype=torch.float64, device=dev)
