@@ -556,7 +556,7 @@ def main():
                 "kernel_pairs_per_s": kern_pairs_s,
                 "kernel_ms_per_launch": kern_ms / max(kern_launches, 1),
                 "kernel_launches": kern_launches}
-    # the same kernel against the driver-measured copy bandwidth and bf16 GEMM rate: it
+    # the same kernel against the measured copy bandwidth and bf16 GEMM rate: it
     # moves ~1e-4 bytes per pair and runs 4 TF32 MMAs of K = 8 per pair (64 FLOP; TF32
     # issues at half the bf16 rate), far from both
     peaks_path = os.path.join(REPO, "MEASURED_PEAKS.json")
