@@ -7,7 +7,8 @@ pitch, z = 0.35 m, Gaussian-blob amplitudes, uniform phases, seed 0) through a
 2.75e11 pair evaluations each, split-FP32 precision, normalised polar outputs.
 
   value     pair-evals/s with inputs resident in HBM (holo_project on device buffers)
-  e2e       the same through the C ABI with host buffers (copies inside the timing)
+  e2e       the same through the C ABI with page-locked host buffers (copies inside
+            the timing)
   roofline  the pair kernel's lane-op rate on its busier pipe (FP32 FMA or XU/MUFU;
             ops per pair from the planned variant's pair model and sin/cos split)
             against that pipe's rate on this GPU measured by holo_probe_peak
@@ -501,13 +502,16 @@ def main():
     total_s = slowest_rank_seconds(sum(step_ms) * 1e-3, world, dev)
     value = whole_job_rate(pairs_step * args.steps, world, total_s)
 
-    # e2e: the C ABI with host buffers, copies inside the timing
+    # e2e: the C ABI with page-locked host buffers, copies inside the timing (the outputs
+    # are page-locked too: the API allocates them like the inputs)
     e2e_steps = max(1, min(args.steps, 3))
-    holo.project(amp, phase, u, v, w, LAM, precision=args.precision)
+    host = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64).reshape(-1)).pin_memory()
+            for a in (amp, phase, u, v, w)]
+    holo.project(*host, LAM, precision=args.precision)
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        holo.project(amp, phase, u, v, w, LAM, precision=args.precision)
+        holo.project(*host, LAM, precision=args.precision)
     barrier()
     e2e_s = slowest_rank_seconds((time.perf_counter() - t0) / e2e_steps, world, dev)
     h2d = 8 * (2 * N + 3 * N + 3 * M + 3 * P)

@@ -77,12 +77,21 @@ class _Buf:
             raise ValueError(f"{name}: expected {count} values, got {self.n}")
 
 
+def _is_pinned(t) -> bool:
+    try:
+        return bool(t.is_pinned())
+    except RuntimeError:  # no accelerator to ask
+        return False
+
+
 def _empty_like(ref: _Buf, count: int):
     if ref.device:
         t = torch.empty(count, dtype=torch.float64, device=f"cuda:{ref.dev_index}")
         return t, t.data_ptr()
     if _is_tensor(ref.obj):
-        t = torch.empty(count, dtype=torch.float64)
+        # page-locked inputs get page-locked outputs: the library's device-to-host copies
+        # then run at the link's rate instead of through the driver's staging buffer
+        t = torch.empty(count, dtype=torch.float64, pin_memory=_is_pinned(ref.obj))
         return t, t.data_ptr()
     a = np.empty(count, dtype=np.float64)
     return a, a.ctypes.data

@@ -63,6 +63,22 @@ def test_project_chain_matches_oracle(holo, orc, prec):
     assert np.max(ya) == pytest.approx(1.0) and np.max(za) == pytest.approx(1.0)
 
 
+def test_project_pinned_host_buffers(holo):
+    """Page-locked CPU inputs: the outputs come back page-locked, complete when the call
+    returns (the copies are asynchronous) and equal to the device-resident call's."""
+    import torch
+    amp, phase, u, v, w = chain64(seed=7)
+    u, v, w = u[:2048], v[:8192], w[:1024]
+    amp, phase = amp[:2048], phase[:2048]
+    host = [torch.from_numpy(np.ascontiguousarray(a).reshape(-1)).pin_memory()
+            for a in (amp, phase, u, v, w)]
+    outs = holo.project(*host, LAM, precision="split32")
+    assert all(o.is_pinned() and not o.is_cuda for o in outs)
+    dev = holo.project(*[h.cuda() for h in host], LAM, precision="split32")
+    for o, d in zip(outs, dev):
+        assert np.array_equal(o.numpy(), d.cpu().numpy())
+
+
 @pytest.mark.parametrize("prec", ["fp64", "split32"])
 @pytest.mark.parametrize("n,m", [(1, 1), (1, 3000), (7, 5), (513, 2049), (3000, 1),
                                  (1025, 777)])
