@@ -16,6 +16,9 @@
  *   - pointers are either all device pointers (the call is asynchronous on
  *     `stream`) or all host pointers (the call copies in and out and returns
  *     when the results are in host memory).  Mixing the two is rejected.
+ *     Host buffers in page-locked memory (cudaHostAlloc / cudaHostRegister)
+ *     are copied at the host link's rate; pageable ones go through the CUDA
+ *     driver's staging buffer (1.1 ms more per 63 MB on GB300).
  *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
  *   - calls on one handle are serialised internally; use one handle per host
  *     thread for concurrency.
