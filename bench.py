@@ -216,7 +216,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "pair-evals/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, config-2 shapes)",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, chain512 shapes)",
         "config": {"workload": WORKLOAD, "sample": f"{n_y} y-pass + {n_z} z-pass targets per step"},
         "cpu_baseline": {"value": value, "unit": "pair-evals/s", "cores": threads, "kind": "port",
                          "sample": f"{n_y} y targets x {len(amp)} sources + {n_z} z targets x "
@@ -230,7 +230,7 @@ def run_reference(args):
 
 
 def run_profile_case(args):
-    """Two launches of the pair kernel on a config-2 slice (the second is the one to capture)."""
+    """Two launches of the pair kernel on a slice of the chain512 y pass (512^2 -> 256^2 of the projector) (the second is the one to capture)."""
     import torch
     import __graft_entry__ as entry
     entry._load_build_module().build()
@@ -382,7 +382,7 @@ def run_other_workload(args):
 
 
 def run_sweep(args):
-    """One JSON line per split-FP32 variant: pair kernel rate on the config-2 y pass."""
+    """One JSON line per split-FP32 variant: pair kernel rate on the chain512 y pass (512^2 -> 1024^2)."""
     import torch
     import __graft_entry__ as entry
     entry._load_build_module().build()
@@ -431,7 +431,7 @@ def main():
                     help="comma-separated variant numbers to restrict --sweep-variants to "
                          "(--profile-case: the first one is forced)")
     ap.add_argument("--sweep-variants", action="store_true",
-                    help="time every split-FP32 kernel variant on the config-2 y pass, then exit")
+                    help="time every split-FP32 kernel variant on the chain512 y pass, then exit")
     ap.add_argument("--workload", default="chain512",
                     choices=["chain512", "chain64", "mc16", "batch64", "adam1024"],
                     help="chain512 (default) is the headline line; the others print their own "
@@ -612,7 +612,7 @@ def main():
         "steps": args.steps, "warmup": max(args.warmup, 3),
         "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if args.precision == "split32" else "f64",
-        "data": "synthetic (seeded; config-2 shapes and value distributions)",
+        "data": "synthetic (seeded; chain512 shapes and value distributions)",
         "config": {"workload": WORKLOAD, "precision": args.precision, "lambda_m": LAM,
                    "pairs_per_step": pairs_step, "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
