@@ -230,7 +230,8 @@ def run_reference(args):
 
 
 def run_profile_case(args):
-    """Two launches of the pair kernel on a slice of the chain512 y pass (512^2 -> 256^2 of the projector) (the second is the one to capture)."""
+    """Two launches of the pair kernel on a slice of the chain512 y pass (512^2 sources
+    onto the central 256^2 of the projector); the second is the one to capture."""
     import torch
     import __graft_entry__ as entry
     entry._load_build_module().build()
