@@ -311,41 +311,57 @@ struct Runner {
     return 0;
   }
 
-  // Forward passes from one source set to several target planes (the
-  // projection planes of -Z): one batched launch over all planes, then each
-  // plane normalised to polar.  *dt is the time of the whole stack.
-  int stack(const std::vector<double> &amp, const std::vector<double> &phase,
-            const std::vector<double> &u, const std::vector<std::vector<double>> &ws,
+  // Timed passes of independent problems (sources k -> targets k) as one batched
+  // launch, each result normalised to polar; an array that several problems share
+  // (the sources of a -Z stack) is uploaded once.  *dt is the time of the whole batch.
+  struct Src {
+    const std::vector<double> *amp, *phase, *pos;
+  };
+  int batch(int sign, const std::vector<Src> &src,
+            const std::vector<const std::vector<double> *> &tgt,
             std::vector<std::vector<double>> *oa, std::vector<std::vector<double>> *op,
             double *dt) {
-    const size_t N = amp.size(), P = ws.size();
+    const size_t P = src.size();
     std::vector<void *> bufs;
+    struct Up {
+      const double *host;
+      size_t n;
+      double *dev;
+    };
+    std::vector<Up> uploaded;
     bool ok = true;
-    auto dev = [&](const double *src, size_t n) -> double * {
+    auto dev = [&](const double *hsrc, size_t n) -> double * {
       void *d = nullptr;
       if (cudaMalloc(&d, (n ? n : 1) * sizeof(double)) != cudaSuccess) {
         ok = false;
         return nullptr;
       }
       bufs.push_back(d);
-      if (src && n && cudaMemcpy(d, src, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      if (hsrc && n && cudaMemcpy(d, hsrc, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
         ok = false;
       return static_cast<double *>(d);
+    };
+    auto up = [&](const std::vector<double> &hv) -> double * {
+      for (const Up &e : uploaded)
+        if (e.host == hv.data() && e.n == hv.size()) return e.dev;
+      double *d = dev(hv.data(), hv.size());
+      uploaded.push_back({hv.data(), hv.size(), d});
+      return d;
     };
     auto release = [&]() {
       for (void *d : bufs) cudaFree(d);
     };
     const double t0 = now();
-    double *da = dev(amp.data(), N), *dp = dev(phase.data(), N), *du = dev(u.data(), 3 * N);
     std::vector<holo_problem> probs(P);
-    for (size_t j = 0; j < P && ok; ++j) {
-      const size_t M = ws[j].size() / 3;
-      double *dw = dev(ws[j].data(), 3 * M), *dz = dev(nullptr, 2 * M);
-      probs[j] = holo_problem{da, dp, du, N, dw, M, HOLO_FORWARDS, p.lambda, dz};
+    for (size_t k = 0; k < P && ok; ++k) {
+      const size_t N = src[k].amp->size(), M = tgt[k]->size() / 3;
+      double *da = up(*src[k].amp), *dp = up(*src[k].phase), *du = up(*src[k].pos);
+      double *dw = up(*tgt[k]), *dz = dev(nullptr, 2 * M);
+      probs[k] = holo_problem{da, dp, du, N, dw, M, sign, p.lambda, dz};
     }
     if (!ok) {
       release();
-      fprintf(stderr, "holo: device buffers for the plane stack: %s\n",
+      fprintf(stderr, "holo: device buffers for the plane batch: %s\n",
               cudaGetErrorString(cudaGetLastError()));
       return 3;
     }
@@ -356,22 +372,22 @@ struct Runner {
     }
     oa->assign(P, {});
     op->assign(P, {});
-    for (size_t j = 0; j < P && rc == 0; ++j) {
-      const size_t M = probs[j].M;
+    for (size_t k = 0; k < P && rc == 0; ++k) {
+      const size_t M = probs[k].M;
       std::vector<double> z(2 * M);
-      if (cudaMemcpy(z.data(), probs[j].y_re_im, 2 * M * sizeof(double),
+      if (cudaMemcpy(z.data(), probs[k].y_re_im, 2 * M * sizeof(double),
                      cudaMemcpyDeviceToHost) != cudaSuccess) {
-        fprintf(stderr, "holo: copy of plane %zu failed\n", j);
+        fprintf(stderr, "holo: copy of plane %zu failed\n", k);
         rc = 3;
         break;
       }
-      (*oa)[j].assign(M, 0.0);
-      (*op)[j].assign(M, 0.0);
-      rc = holo_normalize_polar(h, z.data(), M, (*oa)[j].data(), (*op)[j].data(), nullptr,
+      (*oa)[k].assign(M, 0.0);
+      (*op)[k].assign(M, 0.0);
+      rc = holo_normalize_polar(h, z.data(), M, (*oa)[k].data(), (*op)[k].data(), nullptr,
                                 nullptr);
       if (rc) {
         rc = lib_fail("holo_normalize_polar", rc);
-      } else if (!finite_all((*oa)[j]) || !finite_all((*op)[j])) {
+      } else if (!finite_all((*oa)[k]) || !finite_all((*op)[k])) {
         fprintf(stderr, "holo: non-finite output\n");
         rc = 4;
       }
@@ -453,36 +469,42 @@ int file_mode(Runner &R, const Params &p) {
 }
 
 int generated_mode(Runner &R, const Params &p) {
-  std::vector<double> u(3 * p.n_obj), v(3 * p.n_projector), w(3 * p.n_projection);
+  std::vector<double> u(3 * p.n_obj), w(3 * p.n_projection);
   std::vector<double> xa(p.n_obj, 1.0), xp(p.n_obj, 0.0);
   // descending amplitudes: linspace(N, 1, 0) (cuda/main.cu:66-71, cuda/algebra.h linspace)
   if (p.n_obj > 1) {
     const double delta = (0.0 - 1.0) / (p.n_obj - 1.0);
     for (size_t i = 0; i < p.n_obj; ++i) xa[i] = 1.0 + delta * i;
   }
+  // Every plane's points first, in the reference's order (object, projector lattice,
+  // then its projection lattices: the -r seeds advance in that order), then the passes:
+  // the object planes' x -> y passes as one batched launch, all their projection
+  // planes' y -> z passes as another (cuda/main.cu:125-199 runs one pass at a time;
+  // Monte Carlo and the amplitude-only projector keep one pass each), then the files
+  // in the reference's order.
+  struct XPlane {
+    std::vector<double> u, v, ya, yp;
+    holo_io::Plane x_plane, y_plane;
+    std::vector<std::vector<double>> ws, zas, zps;
+    std::vector<holo_io::Plane> zpl;
+    double dt_y = 0.0, dt_z = 0.0;
+  };
+  std::vector<XPlane> X(p.planes_obj);
   for (size_t i = 0; i < p.planes_obj; ++i) {
     const double ratio = i == 0 ? 0.0 : i / ((double)p.planes_obj - 1.);
     const double obj_off[3] = {lerp(p.off_x, ratio), lerp(p.off_y, ratio), gerp(p.off_z, ratio)};
-    holo_io::Plane x_plane{lerp(p.obj_width, ratio), {obj_off[0], obj_off[1], obj_off[2]}, 1.0,
-                           false};
-    if (!object_points(u, p.shape, x_plane.width, obj_off, i / (double)p.planes_obj))
+    XPlane &P = X[i];
+    P.x_plane = holo_io::Plane{lerp(p.obj_width, ratio), {obj_off[0], obj_off[1], obj_off[2]},
+                               1.0, false};
+    // u carries over from the previous plane: line shapes set x only and the dotted
+    // circle keeps point 0
+    if (!object_points(u, p.shape, P.x_plane.width, obj_off, i / (double)p.planes_obj))
       return lib_fail("object points", -2);
-    holo_io::Plane y_plane{lerp(p.projector_width, ratio), {0, 0, 0}, p.aspect_projector,
-                           p.randomize};
-    if (!lattice(v, y_plane)) return lib_fail("projector lattice (CUDA / cuRAND)", -2);
-    const std::string xs = std::to_string(i);
-    int rc;
-    if ((rc = write(xa, xp, u, "x" + xs, "u" + xs, x_plane, 0.0, 0.0, p.out_dir))) return rc;
-    std::vector<double> ya, yp;
-    double dt = 0;
-    if ((rc = R.pass(HOLO_BACKWARDS, xa, xp, u, v, &ya, &yp, &dt, p.amplitude_only))) return rc;
-    if ((rc = write(ya, yp, v, "y" + xs, "v" + xs, y_plane, dt, flops(dt, xa.size(), ya.size()),
-                    p.out_dir)))
-      return rc;
-    // the projection planes (-Z) share the sources y: with more than one they
-    // run as one batched launch (Monte Carlo sampling keeps one pass each)
-    std::vector<std::vector<double>> ws;
-    std::vector<holo_io::Plane> zpl;
+    P.u = u;
+    P.y_plane = holo_io::Plane{lerp(p.projector_width, ratio), {0, 0, 0}, p.aspect_projector,
+                               p.randomize};
+    P.v.assign(3 * p.n_projector, 0.0);
+    if (!lattice(P.v, P.y_plane)) return lib_fail("projector lattice (CUDA / cuRAND)", -2);
     for (size_t j = 0; j < p.planes_projection; ++j) {
       const double r2 = j == 0 ? 0.0 : j / ((double)p.planes_projection - 1.);
       const double width = gerp(p.projection_width, r2), height = width / p.aspect_projection;
@@ -493,27 +515,75 @@ int generated_mode(Runner &R, const Params &p) {
                              p.aspect_projection,
                              p.randomize};
       if (!lattice(w, z_plane)) return lib_fail("projection lattice (CUDA / cuRAND)", -2);
-      ws.push_back(w);
-      zpl.push_back(z_plane);
+      P.ws.push_back(w);
+      P.zpl.push_back(z_plane);
     }
-    const bool batched = ws.size() > 1 && p.mc_sub == 0;
-    std::vector<std::vector<double>> zas, zps;
-    double dt_plane = 0.0;
-    if (batched) {
-      if ((rc = R.stack(ya, yp, v, ws, &zas, &zps, &dt))) return rc;
-      dt_plane = dt / (double)ws.size();
+  }
+  int rc;
+  // x -> y
+  if (X.size() > 1 && p.mc_sub == 0 && !p.amplitude_only) {
+    std::vector<Runner::Src> src;
+    std::vector<const std::vector<double> *> tgt;
+    for (XPlane &P : X) {
+      src.push_back({&xa, &xp, &P.u});
+      tgt.push_back(&P.v);
     }
-    for (size_t j = 0; j < ws.size(); ++j) {
-      std::vector<double> za, zp;
-      if (batched) {
-        za.swap(zas[j]);
-        zp.swap(zps[j]);
-      } else {
-        if ((rc = R.pass(HOLO_FORWARDS, ya, yp, v, ws[j], &za, &zp, &dt_plane, false))) return rc;
+    std::vector<std::vector<double>> yas, yps;
+    double dt = 0.0;
+    if ((rc = R.batch(HOLO_BACKWARDS, src, tgt, &yas, &yps, &dt))) return rc;
+    for (size_t i = 0; i < X.size(); ++i) {
+      X[i].ya.swap(yas[i]);
+      X[i].yp.swap(yps[i]);
+      X[i].dt_y = dt / (double)X.size();
+    }
+  } else {
+    for (XPlane &P : X)
+      if ((rc = R.pass(HOLO_BACKWARDS, xa, xp, P.u, P.v, &P.ya, &P.yp, &P.dt_y,
+                       p.amplitude_only)))
+        return rc;
+  }
+  // y -> z, every projection plane of every object plane
+  size_t n_z = 0;
+  for (const XPlane &P : X) n_z += P.ws.size();
+  if (n_z > 1 && p.mc_sub == 0) {
+    std::vector<Runner::Src> src;
+    std::vector<const std::vector<double> *> tgt;
+    for (XPlane &P : X)
+      for (const std::vector<double> &wj : P.ws) {
+        src.push_back({&P.ya, &P.yp, &P.v});
+        tgt.push_back(&wj);
       }
+    std::vector<std::vector<double>> zas, zps;
+    double dt = 0.0;
+    if ((rc = R.batch(HOLO_FORWARDS, src, tgt, &zas, &zps, &dt))) return rc;
+    size_t k = 0;
+    for (XPlane &P : X) {
+      P.dt_z = dt / (double)n_z;
+      for (size_t j = 0; j < P.ws.size(); ++j, ++k) {
+        P.zas.push_back(std::move(zas[k]));
+        P.zps.push_back(std::move(zps[k]));
+      }
+    }
+  } else {
+    for (XPlane &P : X)
+      for (const std::vector<double> &wj : P.ws) {
+        std::vector<double> za, zp;
+        if ((rc = R.pass(HOLO_FORWARDS, P.ya, P.yp, P.v, wj, &za, &zp, &P.dt_z, false))) return rc;
+        P.zas.push_back(std::move(za));
+        P.zps.push_back(std::move(zp));
+      }
+  }
+  for (size_t i = 0; i < X.size(); ++i) {
+    const XPlane &P = X[i];
+    const std::string xs = std::to_string(i);
+    if ((rc = write(xa, xp, P.u, "x" + xs, "u" + xs, P.x_plane, 0.0, 0.0, p.out_dir))) return rc;
+    if ((rc = write(P.ya, P.yp, P.v, "y" + xs, "v" + xs, P.y_plane, P.dt_y,
+                    flops(P.dt_y, xa.size(), P.ya.size()), p.out_dir)))
+      return rc;
+    for (size_t j = 0; j < P.ws.size(); ++j) {
       const std::string zs = xs + "_" + std::to_string(j);
-      if ((rc = write(za, zp, ws[j], "z" + zs, "w" + zs, zpl[j], dt_plane,
-                      flops(dt_plane, ya.size(), za.size()), p.out_dir)))
+      if ((rc = write(P.zas[j], P.zps[j], P.ws[j], "z" + zs, "w" + zs, P.zpl[j], P.dt_z,
+                      flops(P.dt_z, P.ya.size(), P.zas[j].size()), p.out_dir)))
         return rc;
     }
   }

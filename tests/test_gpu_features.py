@@ -262,6 +262,42 @@ def test_cli_generated_mode(holo, tmp_path):
         assert zf.size == 1024 and np.max(np.abs(zf - za)) < 1e-4
 
 
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("split32", 1e-4)])
+def test_cli_generated_plane_sweep(holo, tmp_path, prec, tol):
+    """-X 3 -Z 2 (cuda/main.cu:125-199): three object planes of different width, height and
+    projector width; their x -> y passes run as one batched launch and their six y -> z
+    passes as another.  Files and metadata come out in the reference's per-plane order, and
+    every plane equals its own single pass."""
+    r = subprocess.run([_cli(holo), "-x", "16", "-y", "4096", "-z", "1024", "-X", "3", "-Z", "2",
+                        "-o", "1e-4", "-O", "3e-4", "-l", "3e-3", "-L", "4e-3", "-w", "0.3",
+                        "-W", "0.4", "--out", str(tmp_path), "--precision", prec],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    meta = holo.io.parse_out_json(str(tmp_path / "out.json"))
+    assert [m["phasor"] for m in meta] == [n for i in range(3)
+                                           for n in (f"x{i}", f"y{i}", f"z{i}_0", f"z{i}_1")]
+    rd = lambda name: holo.io.read_dat(str(tmp_path / name))
+
+    def norm_polar(y):
+        return np.abs(y) / np.abs(y).max(), np.angle(y)
+
+    z_heights = []
+    for i in range(3):
+        xa, xp = rd(f"x{i}_amp.dat"), rd(f"x{i}_phase.dat")
+        u, v = rd(f"u{i}.dat").reshape(-1, 3), rd(f"v{i}.dat").reshape(-1, 3)
+        z_heights.append(u[0, 2])
+        ya, yp = rd(f"y{i}_amp.dat"), rd(f"y{i}_phase.dat")
+        ea, _ = norm_polar(holo.transform(xa, xp, u, v, -1, 0.65e-6, precision="fp64"))
+        assert np.max(np.abs(ya - ea)) < tol
+        for j in range(2):
+            w = rd(f"w{i}_{j}.dat").reshape(-1, 3)
+            za = rd(f"z{i}_{j}_amp.dat")
+            qa, _ = norm_polar(holo.transform(ya, yp, v, w, +1, 0.65e-6, precision="fp64"))
+            assert za.size == 1024 and np.max(np.abs(za - qa)) < tol
+    assert z_heights[0] == pytest.approx(0.3) and z_heights[2] == pytest.approx(0.4)
+    assert not np.array_equal(rd("v0.dat"), rd("v2.dat"))
+
+
 def test_cli_generated_lattices(holo, tmp_path):
     """The projector lattice of the generated-data mode, built on the device
     (cuda/init.h:89-158): cell centres of a 64 x 64 grid over the 3.584 mm default width
