@@ -210,6 +210,69 @@ def test_invalid_arguments_return_status(holo):
     holo.handle(0).status()  # nothing left on the device error word
 
 
+@pytest.mark.parametrize("prec", ["fp64", "split32"])
+@pytest.mark.parametrize("on_device", [False, True])
+def test_empty_inputs(holo, prec, on_device):
+    """No sources: every target's sum is the empty sum 0; no targets: an empty result."""
+    import torch
+    if on_device:
+        put = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device="cuda:0")
+    else:
+        put = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    e = np.zeros(0)
+    v = grid(10, 7.56e-6, 0.0)
+    y = holo.transform(put(e), put(e), put(e), put(v), -1, LAM, precision=prec)
+    y = y.cpu().numpy() if on_device else y
+    assert y.shape == (100,) and np.all(y == 0)
+    u = grid(4, 10e-6, 0.35)
+    y = holo.transform(put(np.ones(16)), put(np.zeros(16)), put(u), put(e), -1, LAM,
+                       precision=prec)
+    assert tuple(y.shape) == (0,)
+    holo.handle(0).status()
+
+
+def test_maximum_point_counts(holo):
+    """The largest planes the tiler takes, 4096 x 4096 points per side: that many targets
+    from 64 sources, and that many sources onto 256 targets, match the FP64 kernel (the
+    oracle at this size, itself checked against the C oracle above) within the split
+    tolerance.  One point more on either side is rejected with HOLO_ERR_INVALID; the
+    buffers are real and of the claimed size, so nothing could be read out of bounds even
+    if the check were missing."""
+    import torch
+    lim = 4096 * 4096
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(40)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+
+    def check(u, v):
+        n = len(u)
+        amp, phase = t(rng.uniform(0, 1, n)), t(rng.uniform(0, 2 * np.pi, n))
+        y32 = holo.transform(amp, phase, t(u), t(v), -1, LAM, precision="split32")
+        y64 = holo.transform(amp, phase, t(u), t(v), -1, LAM, precision="fp64")
+        err = float(torch.linalg.vector_norm(y32 - y64) / torch.linalg.vector_norm(y64))
+        assert y32.numel() == len(v) and err < 1e-5, err
+
+    check(grid(8, 10e-6, 0.35), grid(4096, 7.56e-6, 0.0))  # 64 -> 4096^2
+    check(grid(4096, 10e-6, 0.35), grid(16, 7.56e-6, 0.0))  # 4096^2 -> 256
+    torch.cuda.empty_cache()
+
+    over = lim + 1
+    src = t(grid(8, 10e-6, 0.35))
+    amp, phase = t(np.ones(64)), t(np.zeros(64))
+    with pytest.raises(holo.HoloError) as e:  # M above the limit
+        holo.transform(amp, phase, src, torch.zeros(3 * over, dtype=torch.float64, device=dev),
+                       -1, LAM, precision="split32")
+    assert e.value.code == holo._native.ERR_INVALID and "supported" in str(e.value)
+    u_over = torch.zeros(over, 3, dtype=torch.float64, device=dev)
+    u_over[:, 2] = 0.35
+    with pytest.raises(holo.HoloError) as e:  # N above the limit
+        holo.transform(torch.ones(over, dtype=torch.float64, device=dev),
+                       torch.zeros(over, dtype=torch.float64, device=dev), u_over,
+                       t(grid(16, 7.56e-6, 0.0)), -1, LAM, precision="split32")
+    assert e.value.code == holo._native.ERR_INVALID and "supported" in str(e.value)
+    holo.handle(0).status()
+
+
 def test_reference_wave_amplitude_only(holo, orc):
     """PROJECT_PHASE=0 path (cuda/transform.cu:379-395) restated with the oracle."""
     amp, phase, u, v, _ = chain64(seed=6)
