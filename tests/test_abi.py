@@ -34,6 +34,25 @@ def test_library_exports_every_declared_symbol(holo):
     assert set(declared_functions()) <= set(holo._native.SIGNATURES)
 
 
+def test_header_is_plain_c_and_links(holo, tmp_path):
+    """A C caller (the binding a cgo or FFI stub compiles against): the header is C99
+    without warnings, and a program linked to libholo.so gets a status, never an exit,
+    when there is no GPU to run on."""
+    src = tmp_path / "caller.c"
+    src.write_text('#include <stdio.h>\n#include "holo.h"\n'
+                   "int main(void) {\n  holo_handle h;\n  int rc = holo_create(0, &h);\n"
+                   "  if (rc == HOLO_OK) { holo_destroy(h); return 0; }\n"
+                   '  printf("%d %s\\n", rc, holo_last_error_string());\n  return 0;\n}\n')
+    lib_dir = os.path.dirname(holo._native.LIB_PATH)
+    exe = tmp_path / "caller"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                        "-I", os.path.join(REPO, "include"), str(src), "-L", lib_dir, "-lholo",
+                        f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_abi_version(holo):
     assert holo._native.load().holo_abi_version() == 1
 
