@@ -37,3 +37,24 @@ def test_every_split_variant_has_a_pipe_model(holo):
     for v in holo.variants("split32"):
         mufu, fp32 = bench.pipe_ops_per_pair(v)
         assert 0.0 <= mufu <= 3.0 and 2.0 <= fp32 <= 28.0, v
+
+
+def test_profile_commands_use_committed_files_and_live_flags():
+    """Every command quoted in profiles/ runs bench.py with options it still has."""
+    import glob
+    import re
+    import subprocess
+    help_text = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--help"],
+                               capture_output=True, text=True, check=True).stdout
+    flags = set(re.findall(r"(--[a-z][a-z0-9-]*)", help_text))
+    seen = 0
+    for path in glob.glob(os.path.join(REPO, "profiles", "*.md")):
+        text = open(path).read()
+        assert "ncu " in text and "--clock-control none" in text, path
+        for cmd in re.findall(r"python (\S+\.py)((?: --?[a-z0-9-]+(?: [0-9]+)?)*)", text):
+            script, args = cmd
+            assert os.path.exists(os.path.join(REPO, script)), (path, script)
+            for flag in re.findall(r"--[a-z][a-z0-9-]*", args):
+                assert flag in flags, (path, flag)
+            seen += 1
+    assert seen >= 4
