@@ -436,7 +436,10 @@ def main():
     ap.add_argument("--workload", default="chain512",
                     choices=["chain512", "chain64", "mc16", "batch64", "adam1024"],
                     help="chain512 (default) is the headline line; the others print their own "
-                         "JSON line: 1 FP64 chain, 3 Monte Carlo, 4 batched, 5 Adam hologram")
+                         "JSON line: chain64 the 64^2 -> 256^2 -> 64^2 chain in FP64 and "
+                         "split-FP32, mc16 its x -> y pass with 1/16 of the sources (Monte "
+                         "Carlo), batch64 64 uneven problems batched against one by one, "
+                         "adam1024 100 Adam steps of a 1024^2 phase hologram onto 512^2")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
