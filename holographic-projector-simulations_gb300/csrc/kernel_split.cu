@@ -586,7 +586,7 @@ std::vector<int> split_preferences(size_t N, size_t M) {
   // waste no more than variant 3's, then the CUDA-core model 0 on 512 and 256
   if (M < 1024) return {34, 44, 45, 3, 4};
   // fastest first: the tensor-core phase (pair model 3) on source tiles of 1024,
-  // 512 and 256 (measured on the config-2 y pass: 2.90, 2.70, 2.46e12 pairs/s), then
+  // 512 and 256 (measured on the 512^2 -> 1024^2 y pass: 2.93, 2.71, 2.50e12 pairs/s), then
   // the CUDA-core pair models 2, 1, 0 on ever smaller tiles
   return {34, 44, 45, 23, 13, 9, 27, 21, 16, 11, 3, 4};
 }

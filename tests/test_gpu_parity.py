@@ -293,7 +293,7 @@ def test_reference_wave_amplitude_only(holo, orc):
 @pytest.mark.parametrize("prec", ["fp64", "split32"])
 def test_every_kernel_variant(holo, orc, prec):
     """Each kernel variant (tile shapes, FMA-pipe sin/cos share, curvature term on or off)
-    meets the precision target on a 32x32 -> 64x64 patch of the config-1 planes, both
+    meets the precision target on a 32x32 -> 64x64 patch of the 64^2 -> 256^2 planes, both
     signs.  The variants without the curvature term are exact enough here because the
     planes are 0.35 m apart and the tiles are a fraction of a millimetre wide."""
     rng = np.random.default_rng(11)
