@@ -144,8 +144,9 @@ def test_deterministic(holo, prec):
 
 
 def test_chain512_split_vs_fp64_kernel(holo, orc):
-    """512^2 sources -> 1024^2 projector at full source count: split-FP32 vs the FP64 kernel (validated above against
-    the CPU oracle) on a seeded 4096-target subset, and vs the CPU oracle on 64 targets."""
+    """512^2 sources -> 1024^2 projector at full source count: split-FP32 vs the FP64
+    kernel (validated above against the CPU oracle) on a seeded 4096-target subset, and
+    vs the CPU oracle on 64 targets."""
     import torch
     amp, phase, u, v, _ = chain512()
     rng = np.random.default_rng(1)
