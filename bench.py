@@ -249,7 +249,8 @@ def run_profile_case(args):
         for _ in range(2):
             holo.transform(*args_, -1, LAM, precision=args.precision, variant=var)
         torch.cuda.synchronize()
-        print(json.dumps({"profile_case": {"variant": var}, "pairs_per_launch": len(amp) * len(vv)}))
+        print(json.dumps({"profile_case": {"variant": var},
+                          "pairs_per_launch": len(amp) * len(vv)}))
         return
     with holo.Plan(args_[2], args_[3], args.precision) as pl:
         for _ in range(2):
@@ -378,12 +379,14 @@ def run_other_workload(args):
         out.update({"adam_steps": steps, "seconds": dt, "s_per_step": dt / steps,
                     "pair_evals_per_s": pairs_step * steps / dt, "loss_first": losses[0],
                     "loss_last": losses[-1],
-                    "config": "1024^2 phases -> 512^2 target intensity, forward + adjoint per step"})
+                    "config": "1024^2 phases -> 512^2 target intensity, forward + adjoint "
+                              "per step"})
     print(json.dumps(out), flush=True)
 
 
 def run_sweep(args):
-    """One JSON line per split-FP32 variant: pair kernel rate on the chain512 y pass (512^2 -> 1024^2)."""
+    """One JSON line per split-FP32 variant: pair kernel rate on the chain512 y pass
+    (512^2 -> 1024^2)."""
     import torch
     import __graft_entry__ as entry
     entry._load_build_module().build()
@@ -413,7 +416,8 @@ def run_sweep(args):
             ref = yv
         rate = 2 * len(amp) * len(v) / (ms * 1e-3)
         print(json.dumps({"variant": var, "kernel_pairs_per_s": rate, "ms": ms / n,
-                          "rel_l2_vs_first": float(np.linalg.norm(yv - ref) / np.linalg.norm(ref))}),
+                          "rel_l2_vs_first": float(np.linalg.norm(yv - ref) /
+                                                   np.linalg.norm(ref))}),
               flush=True)
 
 

@@ -23,9 +23,8 @@ LIB = os.path.join(HERE, "libholo.so")
 CLI = os.path.join(HERE, "holo")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_UNITS = ["abi.cu", "batch.cu", "epilogue.cu", "kernel_fp64.cu", "kernel_split.cu", "kernel_tc.cu",
-             "noalloc.cu",
-             "probe.cu", "tiler.cu"]
+LIB_UNITS = ["abi.cu", "batch.cu", "epilogue.cu", "kernel_fp64.cu", "kernel_split.cu",
+             "kernel_tc.cu", "noalloc.cu", "probe.cu", "tiler.cu"]
 CLI_UNITS = ["cli.cpp", "io.cpp", "gen.cu"]
 HEADERS = ["internal.cuh", "ptx.cuh", "split_frame.cuh", "io.h", "gen.h"]
 

@@ -153,7 +153,8 @@ def _point_sets():
     yield "10000 identical points", np.tile([[1e-4, -2e-4, 0.3]], (10000, 1))
 
 
-@pytest.mark.parametrize("name,pts", list(_point_sets()), ids=lambda x: x if isinstance(x, str) else "")
+@pytest.mark.parametrize("name,pts", list(_point_sets()),
+                         ids=lambda x: x if isinstance(x, str) else "")
 def test_tile_orders_match_models(holo, name, pts):
     for tiling, model in (("packed", model_order), ("hilbert", hilbert_model_order)):
         order = holo.tile_order(pts, tiling)
