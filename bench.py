@@ -58,6 +58,25 @@ def pipe_ops_per_pair(variant: dict) -> tuple[float, float]:
 
 
 WORKLOAD = "chain512: 512^2 sources -> 1024^2 projector -> 512^2 projection (x->y->z)"
+# committed ncu summaries whose `key: value` lines the roofline reads
+PROF_TRAFFIC = os.path.join(REPO, "profiles", "k_split_traffic_chain512.md")
+PROF_MIX = os.path.join(REPO, "profiles", "k_split_tc_mix_chain512_slice.md")
+PROF_FP64 = os.path.join(REPO, "profiles", "k_fp64_chain512_slice.md")
+
+
+def profile_figures(path: str) -> dict:
+    """The `key: number` lines of a committed profile summary (empty if absent)."""
+    out = {}
+    if not os.path.exists(path):
+        return out
+    for line in open(path):
+        key, sep, val = line.partition(":")
+        if sep and key.strip() and " " not in key.strip():
+            try:
+                out[key.strip()] = float(val.split()[0])
+            except (ValueError, IndexError):
+                pass
+    return out
 
 
 def grid(n, pitch, z):
@@ -157,6 +176,16 @@ def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
     return world * units_per_rank / seconds
 
 
+# The CPU baseline is the repo's C oracle, not the reference's NumPy prototype
+# (py/util.py:92-147): the prototype imports numba and pandas and calls an undefined
+# global, and the reference sources are not on the GPU host.  Measured in the build
+# container (Xeon, 2.7 GHz), the prototype ran 1.35e7 pair-evals/s per core with the
+# minimal import shims, the C oracle 3.5e7: the oracle is the faster baseline.
+PROTOTYPE_NOTE = ("C-oracle substitute for the reference's NumPy prototype (py/util.py:92-147), "
+                  "which ran 1.35e7 pair-evals/s per core where both were measured (the oracle "
+                  "3.5e7); the prototype cannot run on the GPU host")
+
+
 def cpu_baseline(amp, phase, u, v, seconds: float = 12.0) -> dict:
     """The C oracle (FP64, every host thread) on a bounded sample of y-pass targets."""
     import oracle
@@ -174,7 +203,8 @@ def cpu_baseline(amp, phase, u, v, seconds: float = 12.0) -> dict:
     return {"value": n_t * len(amp) / dt, "unit": "pair-evals/s", "cores": threads,
             "kind": "port",
             "sample": f"{n_t} random targets of the y pass x all {len(amp)} sources "
-                      f"(FP64 C oracle, {dt:.1f} s)"}
+                      f"(FP64 C oracle, {dt:.1f} s)",
+            "substitute_for": PROTOTYPE_NOTE}
 
 
 def run_reference(args):
@@ -222,7 +252,8 @@ def run_reference(args):
                          "sample": f"{n_y} y targets x {len(amp)} sources + {n_z} z targets x "
                                    f"{len(v)} sources per step, FP64 C oracle (restatement of "
                                    "cuda/superposition.cu:35-51); the reference's own host code "
-                                   "cannot be built on the GPU host"},
+                                   "cannot be built on the GPU host",
+                         "substitute_for": PROTOTYPE_NOTE},
         "e2e": {"value": value, "unit": "pair-evals/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -282,105 +313,225 @@ def _events_ms(fn, reps=1):
     return e0.elapsed_time(e1) / reps, out
 
 
+def _t(dev):
+    import torch
+    return lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+
+
+def chain64_inputs(seed=0):
+    """64^2 sources (10 um, z = 0.35 m) -> 256^2 projector (7.56 um, z = 0) -> the 64^2
+    grid again; amplitudes U[0,1), phases U[0, 2 pi)."""
+    rng = np.random.default_rng(seed)
+    u = grid(64, 10e-6, 0.35)
+    v = grid(256, 7.56e-6, 0.0)
+    amp = rng.uniform(0, 1, len(u))
+    phase = rng.uniform(0, 2 * np.pi, len(u))
+    return amp, phase, u, v, u.copy()
+
+
+def cpu_chain64(threads=None):
+    """The CPU leg for the 64^2 -> 256^2 -> 64^2 chain: the FP64 C oracle (all host
+    threads) runs the whole chain, normalisation included; its timing is the chain's
+    CPU baseline and its fields the reference the GPU chains are compared with."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.build()
+    threads = threads or os.cpu_count() or 1
+    amp, phase, u, v, w = chain64_inputs()
+    t0 = time.perf_counter()
+    y = oracle.transform(amp, phase, u, v, -1, LAM, threads)
+    yn, _ = oracle.normalize_amp(y)
+    ya, yp = oracle.to_polar(yn)
+    z = oracle.transform(ya, yp, v, w, +1, LAM, threads)
+    zn, _ = oracle.normalize_amp(z)
+    dt = time.perf_counter() - t0
+    pairs = len(amp) * len(v) + len(v) * len(w)
+    return {"seconds": dt, "pair_evals_per_s": pairs / dt, "cores": threads, "kind": "port",
+            "what": "FP64 C oracle (restatement of cuda/superposition.cu:35-51), whole chain"}, \
+        yn, zn
+
+
+def wl_chain64(holo, dev, reps=5, cpu=None):
+    """Both precisions through the one-shot x -> y -> z call (planning included), and
+    the normalised fields against the oracle chain when `cpu` = cpu_chain64() is given."""
+    t = _t(dev)
+    amp, phase, u, v, w = chain64_inputs()
+    d = [t(a) for a in (amp, phase, u, v, w)]
+    pairs = len(u) * len(v) + len(v) * len(w)
+    out = {"pairs_per_chain": pairs,
+           "config": "64^2 sources -> 256^2 projector -> 64^2 projection, lambda 632.8 nm"}
+    for prec in ("fp64", "split32"):
+        holo.project(*d, LAM, precision=prec)
+        ms, r = _events_ms(lambda: holo.project(*d, LAM, precision=prec), reps=reps)
+        ya, yp, za, zp = (x.cpu().numpy() for x in r)
+        row = {"ms_per_chain": ms, "pair_evals_per_s": pairs / (ms * 1e-3)}
+        if cpu is not None:
+            _, yo, zo = cpu
+            yg, zg = ya * np.exp(1j * yp), za * np.exp(1j * zp)
+            row.update({"y_rel_l2_vs_oracle": float(np.linalg.norm(yg - yo) / np.linalg.norm(yo)),
+                        "z_rel_l2_vs_oracle": float(np.linalg.norm(zg - zo) / np.linalg.norm(zo)),
+                        "y_max_phase_err_rad": float(np.max(np.abs(np.angle(yg / yo)))),
+                        "z_max_phase_err_rad": float(np.max(np.abs(np.angle(zg / zo))))})
+        out[prec] = row
+    if cpu is not None:
+        out["cpu_oracle"] = cpu[0]
+        out["split32_over_cpu"] = out["split32"]["pair_evals_per_s"] / cpu[0]["pair_evals_per_s"]
+    return out
+
+
+def wl_mc16(holo, dev, reps=3):
+    """x -> y of the 64^2 -> 256^2 chain with 1/16 of the sources per block of 256
+    targets, against the FP64 brute force on the same targets."""
+    t = _t(dev)
+    amp, phase, u, v, _ = chain64_inputs()
+    d = [t(a) for a in (amp, phase, u, v)]
+    y64 = holo.transform(*d, -1, LAM, precision="fp64").cpu().numpy()
+    holo.transform_mc(*d, -1, LAM, seed=1, subsample=16, targets_per_block=256)
+    ms, ymc = _events_ms(lambda: holo.transform_mc(*d, -1, LAM, seed=2, subsample=16,
+                                                   targets_per_block=256), reps=reps)
+    ymc = ymc.cpu().numpy()
+    ms_bf, _ = _events_ms(lambda: holo.transform(*d, -1, LAM, precision="split32"), reps=reps)
+    return {"mc_ms": ms, "brute_force_split32_ms": ms_bf,
+            "sampled_pair_evals_per_s": len(u) // 16 * len(v) / (ms * 1e-3),
+            "effective_pair_evals_per_s": len(u) * len(v) / (ms * 1e-3),
+            "mc_rel_l2_vs_fp64": float(np.linalg.norm(ymc - y64) / np.linalg.norm(y64)),
+            "mc_expected_rel_l2": mc_expected_rel_l2(amp, u, v, y64, 16),
+            "config": "x->y pass of the 64^2 -> 256^2 chain, 1/16 of the sources per block of "
+                      "256 targets, Philox-seeded, weight 16"}
+
+
+def batch64_problems(dev, seed=0):
+    """64 problems: N log-uniform in [1024, 262144] on square-ish 10 um grids at z0
+    U[0.2, 0.5] m, projectors of 128^2 .. 1024^2 at 7.56 um, amplitudes U[0,1), phases
+    U[0, 2 pi)."""
+    import torch
+    t = _t(dev)
+    rng = np.random.default_rng(seed)
+    host, pairs = [], 0
+    for i in range(64):
+        ns = int(np.exp(rng.uniform(np.log(1024), np.log(262144))))
+        side = int(np.ceil(np.sqrt(ns)))
+        u = grid(side, 10e-6, rng.uniform(0.2, 0.5))[:ns]
+        v = grid(int(rng.choice([128, 256, 512, 1024])), 7.56e-6, 0.0)
+        amp, phase = rng.uniform(0, 1, ns), rng.uniform(0, 2 * np.pi, ns)
+        host.append((amp, phase, u, v))
+        pairs += ns * len(v)
+    probs = [(t(a), t(p), t(u), t(v), torch.zeros(2 * len(v), dtype=torch.float64, device=dev))
+             for a, p, u, v in host]
+    return host, probs, pairs
+
+
+def wl_batch64(holo, dev, reps=3, check_targets=512):
+    """The 64 problems as one batched persistent launch (CUDA graph replay) against
+    launching each problem's planned transform alone; the batch's fields against the
+    FP64 kernel at `check_targets` random targets of every problem."""
+    import torch
+    host, probs, pairs = batch64_problems(dev)
+    P = [holo.Problem(a, p, u, v, -1, LAM, y) for a, p, u, v, y in probs]
+    with holo.Batch(P, "split32") as b:
+        b.execute()
+        ms_b, _ = _events_ms(b.execute, reps=reps)
+    plans = [holo.Plan(p.u, p.v, "split32") for p in P]
+    for pl, p in zip(plans, P):
+        pl.execute(p.amp, p.phase, -1, LAM)
+    ms_s, _ = _events_ms(lambda: [pl.execute(p.amp, p.phase, -1, LAM)
+                                  for pl, p in zip(plans, P)], reps=max(1, reps - 1))
+    variants = sorted({pl.info()["variant"] for pl in plans})
+    for pl in plans:
+        pl.close()
+    rng = np.random.default_rng(3)
+    errs, phase_errs = [], []
+    for (amp, phase, u, v), (_, _, _, _, y) in zip(host, probs):
+        idx = np.sort(rng.choice(len(v), min(check_targets, len(v)), replace=False))
+        yb = y.cpu().numpy().view(np.complex128)[idx]
+        y64 = holo.transform(*(_t(dev)(a) for a in (amp, phase, u, v[idx])), -1, LAM,
+                             precision="fp64").cpu().numpy()
+        errs.append(float(np.linalg.norm(yb - y64) / np.linalg.norm(y64)))
+        phase_errs.append(float(np.max(np.abs(np.angle(yb / y64)))))
+    torch.cuda.synchronize()
+    return {"problems": 64, "pairs": pairs, "batched_ms": ms_b, "sequential_ms": ms_s,
+            "batched_pair_evals_per_s": pairs / (ms_b * 1e-3),
+            "sequential_pair_evals_per_s": pairs / (ms_s * 1e-3),
+            "speedup_batched_over_sequential": ms_s / ms_b,
+            "split_vs_fp64_rel_l2_worst": max(errs),
+            "split_vs_fp64_rel_l2_median": float(np.median(errs)),
+            "split_vs_fp64_max_phase_err_rad": max(phase_errs),
+            "check": f"{check_targets} random targets per problem, FP64 kernel",
+            "planned_variants_one_by_one": variants,
+            "config": "N log-uniform [1024, 262144], M in {128^2..1024^2}, z0 U[0.2,0.5] m"}
+
+
+def adam1024_inputs(dev, seed=0):
+    """1024^2 projector pixels (7.56 um, z = 0), 512^2 target grid (10 um, z = 0.35 m),
+    target intensity: 8 Gaussian blobs normalised to unit mean."""
+    t = _t(dev)
+    rng = np.random.default_rng(seed)
+    pp = t(grid(1024, 7.56e-6, 0.0)).reshape(-1, 3)
+    tp = t(grid(512, 10e-6, 0.35)).reshape(-1, 3)
+    n = 512
+    yy, xx = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    img = np.zeros((n, n))
+    for _ in range(8):
+        cx, cy = rng.uniform(0, n, 2)
+        img += rng.uniform(0.2, 1) * np.exp(-((xx - cx) ** 2 + (yy - cy) ** 2) /
+                                             (2 * rng.uniform(5, 40) ** 2))
+    return pp, tp, t((img / img.mean()).ravel())
+
+
+def wl_adam1024(holo, dev, steps=100, warmup=3, reps=3):
+    """100 Adam steps (lr 0.05) of 1024^2 projector phases onto a 512^2 target intensity
+    (forward y -> z + hand-written adjoint per step), then forward, adjoint and the Adam
+    update timed apart with CUDA events."""
+    import torch
+    from holo_gb300 import torch_ops
+    pp, tp, target = adam1024_inputs(dev)
+    # untimed warm-up run: first calls into the autograd engine, Adam and the kernels
+    torch_ops.optimise_phase_hologram(pp, tp, target, LAM, steps=warmup, lr=0.05)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, losses = torch_ops.optimise_phase_hologram(pp, tp, target, LAM, steps=steps, lr=0.05)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    n, m = pp.shape[0], tp.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(1)
+    amp = torch.ones(n, dtype=torch.float64, device=dev)
+    phase = (torch.rand(n, generator=g, dtype=torch.float64) * 2 * np.pi).to(dev)
+    grad_y = torch.randn(2 * m, generator=g, dtype=torch.float64).to(dev)
+    with holo.Plan(pp.reshape(-1), tp.reshape(-1), "split32") as pl:
+        pl.execute(amp, phase, +1, LAM)
+        pl.adjoint(amp, phase, grad_y, +1, LAM)
+        fwd_ms, _ = _events_ms(lambda: pl.execute(amp, phase, +1, LAM), reps=reps)
+        adj_ms, _ = _events_ms(lambda: pl.adjoint(amp, phase, grad_y, +1, LAM), reps=reps)
+    p32 = phase.float().clone().requires_grad_(True)
+    opt = torch.optim.Adam([p32], lr=0.05)
+    p32.grad = torch.randn(n, generator=g).to(dev)
+    opt.step()
+    adam_ms, _ = _events_ms(opt.step, reps=10)
+    return {"adam_steps": steps, "seconds": dt, "s_per_step": dt / steps,
+            "pair_evals_per_s": 2 * n * m * steps / dt,
+            "loss_first": losses[0], "loss_last": losses[-1],
+            "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adam_update_ms": adam_ms,
+            "adjoint_over_forward": adj_ms / fwd_ms,
+            "config": "1024^2 phases -> 512^2 target intensity, forward + adjoint per step"}
+
+
 def run_other_workload(args):
-    """The chain64, mc16, batch64 and adam1024 workloads: one JSON line each (not the
-    headline line)."""
+    """The chain64, mc16, batch64 and adam1024 workloads alone: one JSON line each (the
+    default run carries them in the headline line's extra.workloads)."""
     import torch
     import __graft_entry__ as entry
     entry._load_build_module().build()
     holo = entry.load_package()
-    from holo_gb300 import torch_ops
     dev = torch.device("cuda", 0)
-    t = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
-    rng = np.random.default_rng(0)
-
-    def grid_t(n, pitch, z):
-        return grid(n, pitch, z)
-
     out = {"workload": args.workload, "data": "synthetic (seeded)"}
-    if args.workload in ("chain64", "mc16"):
-        u = grid(64, 10e-6, 0.35)
-        v = grid(256, 7.56e-6, 0.0)
-        amp = rng.uniform(0, 1, len(u))
-        phase = rng.uniform(0, 2 * np.pi, len(u))
-        d = [t(a) for a in (amp, phase, u, v, u)]
-        if args.workload == "chain64":
-            for prec in ("fp64", "split32"):
-                holo.project(*d, LAM, precision=prec)
-                ms, _ = _events_ms(lambda: holo.project(*d, LAM, precision=prec), reps=3)
-                out[prec] = {"ms_per_chain": ms,
-                             "pair_evals_per_s": 2 * len(u) * len(v) / (ms * 1e-3)}
-            out["pairs_per_chain"] = 2 * len(u) * len(v)
-        else:
-            y64 = holo.transform(*d[:4], -1, LAM, precision="fp64").cpu().numpy()
-            holo.transform_mc(*d[:4], -1, LAM, seed=1, subsample=16, targets_per_block=256)
-            ms, ymc = _events_ms(lambda: holo.transform_mc(*d[:4], -1, LAM, seed=2,
-                                                           subsample=16, targets_per_block=256),
-                                 reps=3)
-            ymc = ymc.cpu().numpy()
-            ms_bf, _ = _events_ms(lambda: holo.transform(*d[:4], -1, LAM, precision="split32"),
-                                  reps=3)
-            out.update({
-                "mc_ms": ms, "brute_force_split32_ms": ms_bf,
-                "sampled_pair_evals_per_s": len(u) // 16 * len(v) / (ms * 1e-3),
-                "effective_pair_evals_per_s": len(u) * len(v) / (ms * 1e-3),
-                "mc_rel_l2_vs_fp64": float(np.linalg.norm(ymc - y64) / np.linalg.norm(y64)),
-                "mc_expected_rel_l2": mc_expected_rel_l2(amp, u, v, y64, 16),
-                "config": "x->y pass of the 64^2 -> 256^2 chain, 1/16 of the sources per block of "
-                          "256 targets"})
+    if args.workload == "chain64":
+        out.update(wl_chain64(holo, dev, cpu=cpu_chain64()))
+    elif args.workload == "mc16":
+        out.update(wl_mc16(holo, dev))
     elif args.workload == "batch64":
-        probs, pairs = [], 0
-        for i in range(64):
-            ns = int(np.exp(rng.uniform(np.log(1024), np.log(262144))))
-            side = int(np.ceil(np.sqrt(ns)))
-            u = grid(side, 10e-6, rng.uniform(0.2, 0.5))[:ns]
-            ms_side = int(rng.choice([128, 256, 512, 1024]))
-            v = grid(ms_side, 7.56e-6, 0.0)
-            amp, phase = rng.uniform(0, 1, ns), rng.uniform(0, 2 * np.pi, ns)
-            y = torch.zeros(2 * len(v), dtype=torch.float64, device=dev)
-            probs.append(holo.Problem(t(amp), t(phase), t(u), t(v), -1, LAM, y))
-            pairs += ns * len(v)
-        with holo.Batch(probs, "split32") as b:
-            b.execute()
-            ms_b, _ = _events_ms(b.execute, reps=3)
-        plans = [holo.Plan(p.u, p.v, "split32") for p in probs]
-        for pl, p in zip(plans, probs):
-            pl.execute(p.amp, p.phase, -1, LAM)
-        ms_s, _ = _events_ms(lambda: [pl.execute(p.amp, p.phase, -1, LAM)
-                                      for pl, p in zip(plans, probs)], reps=2)
-        for pl in plans:
-            pl.close()
-        out.update({"problems": 64, "pairs": pairs, "batched_ms": ms_b, "sequential_ms": ms_s,
-                    "batched_pair_evals_per_s": pairs / (ms_b * 1e-3),
-                    "sequential_pair_evals_per_s": pairs / (ms_s * 1e-3),
-                    "speedup": ms_s / ms_b,
-                    "config": "N log-uniform [1024, 262144], M in {128^2..1024^2}, z0 U[0.2,0.5]"})
-    else:  # adam1024
-        pp = t(grid(1024, 7.56e-6, 0.0)).reshape(-1, 3)
-        tp = t(grid(512, 10e-6, 0.35)).reshape(-1, 3)
-        n = 512
-        yy, xx = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
-        img = np.zeros((n, n))
-        for _ in range(8):
-            cx, cy = rng.uniform(0, n, 2)
-            img += rng.uniform(0.2, 1) * np.exp(-((xx - cx) ** 2 + (yy - cy) ** 2) /
-                                                 (2 * rng.uniform(5, 40) ** 2))
-        target = t((img / img.mean()).ravel())
-        steps = args.steps if args.steps != 5 else 100
-        # untimed warm-up run: first calls into the autograd engine, Adam and the
-        # library's kernels on a fresh process cost seconds once
-        torch_ops.optimise_phase_hologram(pp, tp, target, LAM, steps=max(3, args.warmup), lr=0.05)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        _, losses = torch_ops.optimise_phase_hologram(pp, tp, target, LAM, steps=steps, lr=0.05)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        pairs_step = 2 * pp.shape[0] * tp.shape[0]
-        out.update({"adam_steps": steps, "seconds": dt, "s_per_step": dt / steps,
-                    "pair_evals_per_s": pairs_step * steps / dt, "loss_first": losses[0],
-                    "loss_last": losses[-1],
-                    "config": "1024^2 phases -> 512^2 target intensity, forward + adjoint "
-                              "per step"})
+        out.update(wl_batch64(holo, dev))
+    else:
+        out.update(wl_adam1024(holo, dev, steps=args.adam_steps))
     print(json.dumps(out), flush=True)
 
 
@@ -429,6 +580,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="split32", choices=["split32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra-workloads", action="store_true",
+                    help="skip the chain64, mc16, batch64 and adam1024 measurements that the "
+                         "default run adds to its line (extra.workloads)")
+    ap.add_argument("--adam-steps", type=int, default=100,
+                    help="Adam steps of the adam1024 workload (default 100)")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: two split-FP32 passes of the 512^2 sources onto "
                          "a 256^2 patch of the projector (1.7e10 pairs each), then exit")
@@ -534,14 +690,20 @@ def main():
     var = next(x for x in holo.variants(args.precision) if x["variant"] == info["variant"]) \
         if args.precision == "split32" else None
     MUFU_PER_PAIR, FP32_PER_PAIR = pipe_ops_per_pair(var) if var else (0.0, 0.0)
+    ops_source = "pair model of the planned variant"
+    # lane-ops per pair counted by ncu on the same variant (XU instructions x 32, FMA-pipe
+    # instructions x 32 with packed f32x2 ones counted twice, per pair evaluated)
+    mix = profile_figures(PROF_MIX)
+    if var and mix.get("variant") == var["variant"] and "xu_lane_ops_per_pair" in mix:
+        MUFU_PER_PAIR = mix["xu_lane_ops_per_pair"]
+        FP32_PER_PAIR = mix["fma_lane_ops_per_pair"]
+        ops_source = "ncu instruction counts (profiles/k_split_tc_mix_chain512_slice.md)"
     achieved = kern_pairs_s * MUFU_PER_PAIR
     # DRAM bytes per pair-kernel launch (the y pass) from the committed ncu capture
     traffic = None
-    prof = os.path.join(REPO, "profiles", "k_split_traffic_chain512.md")
-    if os.path.exists(prof) and args.precision == "split32":
-        for line in open(prof):
-            if line.startswith("bytes_per_launch_y_pass:"):
-                traffic = int(line.split(":")[1])
+    if args.precision == "split32":
+        traffic = profile_figures(PROF_TRAFFIC).get("bytes_per_launch_y_pass")
+        traffic = int(traffic) if traffic else None
     # the pair rate this variant could reach if its busiest pipe ran at the measured peak
     bound_rate = min(mufu_peak / MUFU_PER_PAIR if MUFU_PER_PAIR else float("inf"),
                      ffma_peak / FP32_PER_PAIR if FP32_PER_PAIR else float("inf")) if var else None
@@ -562,6 +724,7 @@ def main():
                 "xu_frac": xu_frac, "xu_achieved_gops": achieved / 1e9,
                 "xu_peak_gops": mufu_peak / 1e9,
                 "variant": var, "mufu_per_pair": MUFU_PER_PAIR, "fp32_per_pair": FP32_PER_PAIR,
+                "ops_per_pair_source": ops_source,
                 "fp32_frac": fp32_frac,
                 "fma_peak_gops": ffma_peak / 1e9,
                 "pairs_per_s_frac_of_pipe_bound": kern_pairs_s / bound_rate if bound_rate else None,
@@ -608,13 +771,41 @@ def main():
     rel = float(np.linalg.norm(a32 - a64) / np.linalg.norm(a64))
     phase_err = float(np.max(np.abs(np.angle(a32 / a64))))
     h.status()
+    # roofline of the FP64 kernel: its FP64-pipe lane-ops per pair (ncu count on a slice of
+    # the same y pass) at the measured pair rate, against the DFMA probe's rate
+    dfma_peak = h.probe_peak(3)
+    f64 = profile_figures(PROF_FP64)
+    fp64_roofline = {"bound": "fp64", "pair_evals_per_s": fp64_rate, "peak_gops": dfma_peak / 1e9,
+                     "unit": "Gop/s", "peak_source": "holo_probe_peak kind 3 (DFMA chains)"}
+    if "fp64_pipe_slots_per_pair" in f64:
+        # pipe slots: the DFMA/DADD/DMUL arithmetic plus the pipe's other FP64 instructions
+        ops = f64["fp64_pipe_slots_per_pair"]
+        fp64_roofline.update({"fp64_pipe_slots_per_pair": ops,
+                              "fp64_arith_per_pair": f64.get("fp64_lane_ops_per_pair"),
+                              "achieved_gops": fp64_rate * ops / 1e9,
+                              "frac": fp64_rate * ops / dfma_peak if dfma_peak else None,
+                              "ops_per_pair_source": "ncu counters on a slice of the same pass "
+                                                     "(profiles/k_fp64_chain512_slice.md)"})
 
     if rank != 0:
         return
-    cpu = None
+    cpu = cpu64 = None
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         cpu = cpu_baseline(amp, phase, u, v)
+        if world == 1 and not args.no_extra_workloads:
+            cpu64 = cpu_chain64()
+    # the other workloads, measured after the headline (N = 1 only)
+    extra = None
+    if world == 1 and not args.no_extra_workloads:
+        t_extra = time.perf_counter()
+        extra = {"workloads": {
+            "chain64": wl_chain64(holo, dev, cpu=cpu64),
+            "mc16": wl_mc16(holo, dev),
+            "batch64": wl_batch64(holo, dev),
+            "adam1024": wl_adam1024(holo, dev, steps=args.adam_steps)}}
+        extra["seconds"] = time.perf_counter() - t_extra
+        h.status()
     line = {
         "metric": METRIC, "value": value, "unit": "pair-evals/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3),
@@ -632,6 +823,8 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
         "fp64_kernel_pairs_per_s": fp64_rate,
+        "fp64_roofline": fp64_roofline,
+        "fp64_frac": fp64_roofline.get("frac"),
         "split_over_fp64": kern_pairs_s / fp64_rate if fp64_rate else None,
         "rel_l2_split_vs_fp64": rel, "max_phase_err_rad": phase_err,
         "accuracy_check": {"targets": len(idx), "variant": acc_variant,
@@ -640,6 +833,7 @@ def main():
         "wall_s_timed": wall,
         "published_reference_pairs_per_s": {"value": 5.3e10, "what": "reference kernel #2, "
                                             "FP64, Quadro GV100, N=1920x1080 (README figure)"},
+        "extra": extra,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -15,7 +15,10 @@
 // Long options added here: --lambda, --precision fp64|split32, --mc SUB,
 // --seed S, --mc-block B, --amplitude-only (PROJECT_PHASE=0), --reference-distance,
 // --ref-compat, --out DIR (generated mode, default ../tmp/ as the reference), --device,
-// --shape (the generated object's shape; the reference fixes it at compile time).
+// --shape (the generated object's shape; the reference fixes it at compile time),
+// --check K (each pass compared with the FP64 kernel at K sampled targets).
+// Every out.json line also carries "pairs_per_s", and with --check "check_targets",
+// "rel_l2" and "max_phase_err", after the reference's keys.
 //
 // Exit codes: 0 success; 2 bad arguments or files; 4 non-finite output (the
 // reference's check_complex exit, cuda/util.h:54-60); 3 a library error.
@@ -27,6 +30,7 @@
 #include <string.h>
 #include <time.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -73,6 +77,7 @@ struct Params {
   bool ref_compat = false;
   std::string out_dir = "../tmp/";
   int device = 0;
+  int check = 0;  // targets per pass compared with the FP64 sum (0: no check)
 };
 
 void show_help(const char *p) {
@@ -113,13 +118,15 @@ void show_help(const char *p) {
       "\t--out DIR             \tOutput directory of the generated mode (default ../tmp/)\n"
       "\t--device D            \tCUDA device\n"
       "\t--shape S             \tGenerated object: circle (default), dotted-circle, line, log-line\n"
+      "\t--check K             \tCompare each pass with the FP64 sum at K sampled targets\n"
+      "\t                      \t(rel_l2 and max_phase_err in out.json)\n"
       "\n",
       p);
 }
 
 bool parse(int argc, char **argv, Params *p, int *exit_code) {
   enum { O_LAMBDA = 1000, O_PREC, O_MC, O_SEED, O_MCB, O_AMP, O_REFD, O_COMPAT, O_OUT, O_DEV,
-         O_SHAPE };
+         O_SHAPE, O_CHECK };
   static struct option longopts[] = {{"lambda", required_argument, 0, O_LAMBDA},
                                      {"precision", required_argument, 0, O_PREC},
                                      {"mc", required_argument, 0, O_MC},
@@ -131,6 +138,7 @@ bool parse(int argc, char **argv, Params *p, int *exit_code) {
                                      {"out", required_argument, 0, O_OUT},
                                      {"device", required_argument, 0, O_DEV},
                                      {"shape", required_argument, 0, O_SHAPE},
+                                     {"check", required_argument, 0, O_CHECK},
                                      {"help", no_argument, 0, 'h'},
                                      {0, 0, 0, 0}};
   int ch;
@@ -180,6 +188,7 @@ bool parse(int argc, char **argv, Params *p, int *exit_code) {
       case O_COMPAT: p->ref_compat = true; break;
       case O_OUT: p->out_dir = std::string(optarg) + "/"; break;
       case O_DEV: p->device = strtol(optarg, 0, 10); break;
+      case O_CHECK: p->check = (int)strtol(optarg, 0, 10); break;
       case O_SHAPE:
         if (!strcmp(optarg, "circle")) p->shape = Shape::Circle;
         else if (!strcmp(optarg, "dotted-circle")) p->shape = Shape::DottedCircle;
@@ -204,6 +213,7 @@ bool parse(int argc, char **argv, Params *p, int *exit_code) {
   else if (p->planes_projection && p->n_projection == 0) bad = "-z must be > 0";
   else if (!(p->lambda > 0.0) || !isfinite(p->lambda)) bad = "--lambda must be > 0";
   else if (p->mc_sub < 0) bad = "--mc must be >= 1";
+  else if (p->check < 0) bad = "--check must be >= 0";
   else if (p->off_z.min > 0 ? !(p->off_z.min > nonzero && p->off_z.max > nonzero)
                             : !(-p->off_z.min > nonzero && -p->off_z.max > nonzero))
     bad = "object z offsets must be nonzero and of one sign";
@@ -278,16 +288,60 @@ bool finite_all(const std::vector<double> &a) {
 struct Runner {
   holo_handle h;
   const Params &p;
-  // One timed pass: sources (amp, phase, pos) -> targets, normalised polar.
+
+  // --check: the FP64 sum at p.check targets spread evenly over the target list
+  // against a computed pass, given as its normalised polar output (oa, op) and
+  // the max |y| it was divided by (the raw field is oa * scale * e^{i op}).
+  int check_field(int sign, const std::vector<double> &amp, const std::vector<double> &phase,
+                  const std::vector<double> &u, const std::vector<double> &v,
+                  const std::vector<double> &oa, const std::vector<double> &op, double max_abs,
+                  holo_io::Extra *ex) {
+    const size_t N = amp.size(), M = v.size() / 3;
+    const size_t K = std::min<size_t>((size_t)p.check, M);
+    if (K == 0) return 0;
+    std::vector<size_t> idx(K);
+    std::vector<double> vs(3 * K), y64(2 * K);
+    for (size_t k = 0; k < K; ++k) {
+      idx[k] = (size_t)(((double)k + 0.5) * (double)M / (double)K);
+      for (int d = 0; d < 3; ++d) vs[3 * k + d] = v[3 * idx[k] + d];
+    }
+    const int rc = holo_transform(h, sign, p.lambda, amp.data(), phase.data(), u.data(), N,
+                                  vs.data(), K, y64.data(), HOLO_FP64, nullptr);
+    if (rc) return lib_fail("holo_transform (--check, FP64)", rc);
+    const double scale = max_abs < 1e-6 ? 1.0 : max_abs;  // as the normalisation did
+    double num = 0.0, den = 0.0, worst = 0.0;
+    for (size_t k = 0; k < K; ++k) {
+      const double a = oa[idx[k]] * scale, ph = op[idx[k]];
+      const double re = a * cos(ph), im = a * sin(ph);
+      const double dr = re - y64[2 * k], di = im - y64[2 * k + 1];
+      num += dr * dr + di * di;
+      den += y64[2 * k] * y64[2 * k] + y64[2 * k + 1] * y64[2 * k + 1];
+      // angle of y / y64
+      const double cr = re * y64[2 * k] + im * y64[2 * k + 1];
+      const double ci = im * y64[2 * k] - re * y64[2 * k + 1];
+      worst = std::max(worst, fabs(atan2(ci, cr)));
+    }
+    ex->checked = true;
+    ex->check_targets = (int)K;
+    ex->rel_l2 = den > 0.0 ? sqrt(num / den) : sqrt(num);
+    ex->max_phase_err = worst;
+    return 0;
+  }
+
+  // One timed pass: sources (amp, phase, pos) -> targets, normalised polar.  `ex`
+  // receives the pair rate and, with --check, the comparison with FP64 (not for the
+  // amplitude-only projector, whose output is not the transform's field).
   int pass(int sign, const std::vector<double> &amp, const std::vector<double> &phase,
            const std::vector<double> &u, const std::vector<double> &v, std::vector<double> *oa,
-           std::vector<double> *op, double *dt, bool reference_wave) {
+           std::vector<double> *op, double *dt, bool reference_wave, holo_io::Extra *ex) {
     const size_t N = amp.size(), M = v.size() / 3;
     oa->assign(M, 0.0);
     op->assign(M, 0.0);
+    double max_abs = 0.0;
+    const bool check = p.check > 0 && !reference_wave;
     const double t0 = now();
     int rc;
-    if (sign == HOLO_BACKWARDS && p.mc_sub == 0) {
+    if (sign == HOLO_BACKWARDS && p.mc_sub == 0 && !check) {
       rc = holo_project(h, p.lambda, amp.data(), phase.data(), u.data(), N, v.data(), M, nullptr,
                         0, oa->data(), op->data(), nullptr, nullptr, p.precision,
                         reference_wave ? 1 : 0, p.reference_distance, nullptr);
@@ -300,7 +354,7 @@ struct Runner {
                : holo_transform(h, sign, p.lambda, amp.data(), phase.data(), u.data(), N,
                                 v.data(), M, y.data(), p.precision, nullptr);
       if (rc) return lib_fail("holo_transform", rc);
-      rc = holo_normalize_polar(h, y.data(), M, oa->data(), op->data(), nullptr, nullptr);
+      rc = holo_normalize_polar(h, y.data(), M, oa->data(), op->data(), &max_abs, nullptr);
       if (rc) return lib_fail("holo_normalize_polar", rc);
     }
     *dt = now() - t0;
@@ -308,6 +362,9 @@ struct Runner {
       fprintf(stderr, "holo: non-finite output\n");
       return 4;
     }
+    *ex = holo_io::Extra();
+    ex->pairs_per_s = *dt > 0.0 ? (double)N * (double)M / *dt : 0.0;
+    if (check) return check_field(sign, amp, phase, u, v, *oa, *op, max_abs, ex);
     return 0;
   }
 
@@ -320,7 +377,7 @@ struct Runner {
   int batch(int sign, const std::vector<Src> &src,
             const std::vector<const std::vector<double> *> &tgt,
             std::vector<std::vector<double>> *oa, std::vector<std::vector<double>> *op,
-            double *dt) {
+            double *dt, std::vector<holo_io::Extra> *ex) {
     const size_t P = src.size();
     std::vector<void *> bufs;
     struct Up {
@@ -372,6 +429,7 @@ struct Runner {
     }
     oa->assign(P, {});
     op->assign(P, {});
+    std::vector<double> max_abs(P, 0.0);
     for (size_t k = 0; k < P && rc == 0; ++k) {
       const size_t M = probs[k].M;
       std::vector<double> z(2 * M);
@@ -383,7 +441,7 @@ struct Runner {
       }
       (*oa)[k].assign(M, 0.0);
       (*op)[k].assign(M, 0.0);
-      rc = holo_normalize_polar(h, z.data(), M, (*oa)[k].data(), (*op)[k].data(), nullptr,
+      rc = holo_normalize_polar(h, z.data(), M, (*oa)[k].data(), (*op)[k].data(), &max_abs[k],
                                 nullptr);
       if (rc) {
         rc = lib_fail("holo_normalize_polar", rc);
@@ -394,15 +452,26 @@ struct Runner {
     }
     *dt = now() - t0;
     release();
+    // every problem is credited with the batch's pair rate (one launch ran them all)
+    double pairs = 0.0;
+    for (size_t k = 0; k < P; ++k) pairs += (double)probs[k].N * (double)probs[k].M;
+    ex->assign(P, holo_io::Extra());
+    for (size_t k = 0; k < P && rc == 0; ++k) {
+      (*ex)[k].pairs_per_s = *dt > 0.0 ? pairs / *dt : 0.0;
+      if (p.check > 0)
+        rc = check_field(sign, *src[k].amp, *src[k].phase, *src[k].pos, *tgt[k], (*oa)[k],
+                         (*op)[k], max_abs[k], &(*ex)[k]);
+    }
     return rc;
   }
 };
 
 int write(const std::vector<double> &a, const std::vector<double> &ph,
           const std::vector<double> &pos, const std::string &k1, const std::string &k2,
-          const holo_io::Plane &pl, double dt, double fl, const std::string &dir) {
+          const holo_io::Plane &pl, double dt, double fl, const std::string &dir,
+          const holo_io::Extra &ex = holo_io::Extra()) {
   std::string err;
-  if (!holo_io::write_arrays(a, ph, pos, k1, k2, pl, dt, fl, dir, &err)) {
+  if (!holo_io::write_arrays(a, ph, pos, k1, k2, pl, dt, fl, ex, dir, &err)) {
     fprintf(stderr, "holo: %s\n", err.c_str());
     return 2;
   }
@@ -449,20 +518,22 @@ int file_mode(Runner &R, const Params &p) {
   (void)x_plane;
   std::vector<double> ya, yp, za, zp;
   double dt = 0;
-  int rc = R.pass(HOLO_BACKWARDS, xa, xp, u, v, &ya, &yp, &dt, p.amplitude_only);
+  holo_io::Extra ex;
+  int rc = R.pass(HOLO_BACKWARDS, xa, xp, u, v, &ya, &yp, &dt, p.amplitude_only, &ex);
   if (rc) return rc;
   printf("y: %zu x %zu pairs in %.6f s (%.3f TFLOPS at 29 FLOP/pair)\n", xa.size(), ya.size(), dt,
          flops(dt, xa.size(), ya.size()) * 1e-12);
-  if ((rc = write(ya, yp, v, "y0", "v0", y_plane, dt, flops(dt, xa.size(), ya.size()), d))) return rc;
+  if ((rc = write(ya, yp, v, "y0", "v0", y_plane, dt, flops(dt, xa.size(), ya.size()), d, ex)))
+    return rc;
   if (p.projection) {
     if (p.ref_compat)
-      rc = R.pass(HOLO_FORWARDS, xa, xp, u, v, &za, &zp, &dt, false);
+      rc = R.pass(HOLO_FORWARDS, xa, xp, u, v, &za, &zp, &dt, false, &ex);
     else
-      rc = R.pass(HOLO_FORWARDS, ya, yp, v, w, &za, &zp, &dt, false);
+      rc = R.pass(HOLO_FORWARDS, ya, yp, v, w, &za, &zp, &dt, false, &ex);
     if (rc) return rc;
     const size_t n_src = p.ref_compat ? xa.size() : ya.size();
     printf("z: %zu x %zu pairs in %.6f s\n", n_src, za.size(), dt);
-    if ((rc = write(za, zp, w, "z0_0", "w0_0", z_plane, dt, flops(dt, n_src, za.size()), d)))
+    if ((rc = write(za, zp, w, "z0_0", "w0_0", z_plane, dt, flops(dt, n_src, za.size()), d, ex)))
       return rc;
   }
   return 0;
@@ -488,6 +559,8 @@ int generated_mode(Runner &R, const Params &p) {
     std::vector<std::vector<double>> ws, zas, zps;
     std::vector<holo_io::Plane> zpl;
     double dt_y = 0.0, dt_z = 0.0;
+    holo_io::Extra ex_y;
+    std::vector<holo_io::Extra> ex_z;
   };
   std::vector<XPlane> X(p.planes_obj);
   for (size_t i = 0; i < p.planes_obj; ++i) {
@@ -529,17 +602,19 @@ int generated_mode(Runner &R, const Params &p) {
       tgt.push_back(&P.v);
     }
     std::vector<std::vector<double>> yas, yps;
+    std::vector<holo_io::Extra> exs;
     double dt = 0.0;
-    if ((rc = R.batch(HOLO_BACKWARDS, src, tgt, &yas, &yps, &dt))) return rc;
+    if ((rc = R.batch(HOLO_BACKWARDS, src, tgt, &yas, &yps, &dt, &exs))) return rc;
     for (size_t i = 0; i < X.size(); ++i) {
       X[i].ya.swap(yas[i]);
       X[i].yp.swap(yps[i]);
       X[i].dt_y = dt / (double)X.size();
+      X[i].ex_y = exs[i];
     }
   } else {
     for (XPlane &P : X)
       if ((rc = R.pass(HOLO_BACKWARDS, xa, xp, P.u, P.v, &P.ya, &P.yp, &P.dt_y,
-                       p.amplitude_only)))
+                       p.amplitude_only, &P.ex_y)))
         return rc;
   }
   // y -> z, every projection plane of every object plane
@@ -554,23 +629,28 @@ int generated_mode(Runner &R, const Params &p) {
         tgt.push_back(&wj);
       }
     std::vector<std::vector<double>> zas, zps;
+    std::vector<holo_io::Extra> exs;
     double dt = 0.0;
-    if ((rc = R.batch(HOLO_FORWARDS, src, tgt, &zas, &zps, &dt))) return rc;
+    if ((rc = R.batch(HOLO_FORWARDS, src, tgt, &zas, &zps, &dt, &exs))) return rc;
     size_t k = 0;
     for (XPlane &P : X) {
       P.dt_z = dt / (double)n_z;
       for (size_t j = 0; j < P.ws.size(); ++j, ++k) {
         P.zas.push_back(std::move(zas[k]));
         P.zps.push_back(std::move(zps[k]));
+        P.ex_z.push_back(exs[k]);
       }
     }
   } else {
     for (XPlane &P : X)
       for (const std::vector<double> &wj : P.ws) {
         std::vector<double> za, zp;
-        if ((rc = R.pass(HOLO_FORWARDS, P.ya, P.yp, P.v, wj, &za, &zp, &P.dt_z, false))) return rc;
+        holo_io::Extra ex;
+        if ((rc = R.pass(HOLO_FORWARDS, P.ya, P.yp, P.v, wj, &za, &zp, &P.dt_z, false, &ex)))
+          return rc;
         P.zas.push_back(std::move(za));
         P.zps.push_back(std::move(zp));
+        P.ex_z.push_back(ex);
       }
   }
   for (size_t i = 0; i < X.size(); ++i) {
@@ -578,12 +658,12 @@ int generated_mode(Runner &R, const Params &p) {
     const std::string xs = std::to_string(i);
     if ((rc = write(xa, xp, P.u, "x" + xs, "u" + xs, P.x_plane, 0.0, 0.0, p.out_dir))) return rc;
     if ((rc = write(P.ya, P.yp, P.v, "y" + xs, "v" + xs, P.y_plane, P.dt_y,
-                    flops(P.dt_y, xa.size(), P.ya.size()), p.out_dir)))
+                    flops(P.dt_y, xa.size(), P.ya.size()), p.out_dir, P.ex_y)))
       return rc;
     for (size_t j = 0; j < P.ws.size(); ++j) {
       const std::string zs = xs + "_" + std::to_string(j);
       if ((rc = write(P.zas[j], P.zps[j], P.ws[j], "z" + zs, "w" + zs, P.zpl[j], P.dt_z,
-                      flops(P.dt_z, P.ya.size(), P.zas[j].size()), p.out_dir)))
+                      flops(P.dt_z, P.ya.size(), P.zas[j].size()), p.out_dir, P.ex_z[j])))
         return rc;
     }
   }

@@ -3,6 +3,12 @@
 // cuda/init.h:160-234), written into device memory and copied to the caller's host
 // vector (the CLI writes them to .dat files too).
 //
+// Every lattice and line coordinate is the reference's host expression evaluated
+// operation by operation with explicitly rounded FP64 intrinsics (no fused
+// multiply-add), so it equals the reference's own output bit for bit; the circle
+// and log-line shapes call CUDA's sin, cos, pow and log10, which differ from a C
+// library's in the last place on some arguments.
+//
 // The lattice's -r jitter takes the reference's cuRAND XORWOW numbers with the same
 // calls in the same order (per row: x + y uniforms, then a second, discarded call of
 // (x + y) / 8), read directly from device memory.  The reference indexes them as
@@ -29,10 +35,12 @@ __global__ void k_lattice(double *__restrict__ v, size_t i0, size_t rows, size_t
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < count;
        q += (size_t)gridDim.x * blockDim.x) {
     const size_t i = i0 + q / y, j = q % y, k = 3 * (j + i * y);
-    double px = i * dx - x_half + ox, py = j * dy - y_half + oy;
-    if (rnd) {
-      px += x_range * (rnd[(2 * j) % n_rnd] - 0.5);
-      py += y_range * (rnd[(2 * j + 1) % n_rnd] - 0.5);
+    // i * dx - x_half + offset.x (cuda/init.h:128-129), left to right
+    double px = __dadd_rn(__dsub_rn(__dmul_rn((double)i, dx), x_half), ox);
+    double py = __dadd_rn(__dsub_rn(__dmul_rn((double)j, dy), y_half), oy);
+    if (rnd) {  // += range * (random - 0.5) (cuda/init.h:133-134)
+      px = __dadd_rn(px, __dmul_rn(x_range, __dsub_rn((double)rnd[(2 * j) % n_rnd], 0.5)));
+      py = __dadd_rn(py, __dmul_rn(y_range, __dsub_rn((double)rnd[(2 * j + 1) % n_rnd], 0.5)));
     }
     v[k] = px;
     v[k + 1] = py;
@@ -60,31 +68,36 @@ __global__ void k_object(double *__restrict__ u, size_t n, int shape, double wid
     }
     const double radius = width / 2.0;
     switch (shape) {
-      case kShapeLine:
-        p[0] = i * (width / (double)(n - 1)) - width / 2.0;
+      case kShapeLine:  // i * du - half_width, du = width / (n - 1) (cuda/init.h:179-185)
+        p[0] = __dsub_rn(__dmul_rn((double)i, __ddiv_rn(width, (double)(n - 1))), width / 2.0);
         break;
       case kShapeLogLine: {
-        // geomspace(n, 1, 1 + width) (cuda/algebra.h:55-91): 10^(linspace of the logs)
-        const double a = log10(1.0), b = log10(1.0 + width), delta = (b - a) / (n - 1.0);
-        p[0] = pow(10.0, a + delta * i) - 1 + width / 2.;
+        // geomspace(n, 1, 1 + width) (cuda/algebra.h:55-91): 10^(a + delta i) over the
+        // logs; then x - 1 + width / 2 (cuda/init.h:188-190)
+        const double a = log10(1.0), b = log10(__dadd_rn(1.0, width));
+        const double delta = __ddiv_rn(__dsub_rn(b, a), __dsub_rn((double)n, 1.0));
+        p[0] = __dadd_rn(__dsub_rn(pow(10.0, __dadd_rn(a, __dmul_rn(delta, (double)i))), 1.0),
+                         width / 2.);
         break;
       }
-      case kShapeCircle: {
-        const double ph = i * (kTwoPi / (double)n) + arbitrary_offset;
-        p[0] = sin(ph) * radius;
-        p[1] = cos(ph) * radius;
+      case kShapeCircle: {  // (cuda/init.h:192-205)
+        const double ph = __dadd_rn(__dmul_rn((double)i, __ddiv_rn(kTwoPi, (double)n)),
+                                    arbitrary_offset);
+        p[0] = __dmul_rn(sin(ph), radius);
+        p[1] = __dmul_rn(cos(ph), radius);
         break;
       }
-      default: {  // dotted circle: point 0 keeps the previous plane's values
+      default: {  // dotted circle: point 0 keeps the previous plane's values (:206-220)
         if (i == 0) break;
-        const double ph = i * (kTwoPi / (double)(n - 1)) + arbitrary_offset;
-        p[0] = sin(ph) * radius;
-        p[1] = cos(ph) * radius;
+        const double ph = __dadd_rn(__dmul_rn((double)i, __ddiv_rn(kTwoPi, (double)(n - 1))),
+                                    arbitrary_offset);
+        p[0] = __dmul_rn(sin(ph), radius);
+        p[1] = __dmul_rn(cos(ph), radius);
       }
     }
     if (ox != 0 || oy != 0) {
-      p[0] += ox;
-      p[1] += oy;
+      p[0] = __dadd_rn(p[0], ox);
+      p[1] = __dadd_rn(p[1], oy);
     }
   }
 }
@@ -102,8 +115,10 @@ int lattice(double *v_host, size_t n, const holo_io::Plane &p, unsigned int seed
   if (x == 0 || y == 0) return -1;
   const double height = p.width / p.aspect_ratio, dx = p.width / (double)x,
                dy = height / (double)y, x_half = (p.width - dx) / 2., y_half = (height - dy) / 2.;
-  const double rel_margin = p.randomize ? 0.05 : 0.0, x_range = dx - 0.5 * rel_margin * dx,
-               y_range = dy - 0.5 * rel_margin * dy;
+  // x_margin = rel_margin dx, x_random_range = dx - 0.5 x_margin (cuda/init.h:109-114)
+  const double rel_margin = p.randomize ? 0.05 : 0.0, x_margin = rel_margin * dx,
+               y_margin = rel_margin * dy, x_range = dx - 0.5 * x_margin,
+               y_range = dy - 0.5 * y_margin;
   const size_t n_random = x + y;
   double *d_v = nullptr;
   float *d_random = nullptr;

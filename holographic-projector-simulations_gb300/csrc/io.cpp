@@ -53,7 +53,7 @@ bool write_dat(const std::string &path, const double *data, size_t count, std::s
 
 std::string metadata_line(const std::string &phasor, const std::string &pos, const Plane &p,
                           const std::vector<double> &amp, const std::vector<double> &phase,
-                          double dt, double flops, long timestamp_ns) {
+                          double dt, double flops, long timestamp_ns, const Extra &extra) {
   // sums in array order (transform_reduce, cuda/algebra.h), default ostream
   // formatting as in the reference (its std::fixed is set after this line)
   double a = 0.0, ph = 0.0;
@@ -77,18 +77,24 @@ std::string metadata_line(const std::string &phasor, const std::string &pos, con
       << "\"aspect_ratio\"" << s1 << p.aspect_ratio << s2
       << "\"timestamp\"" << s1 << timestamp_ns << s2
       << "\"runtime\"" << s1 << dt << s2
-      << "\"flops\"" << s1 << flops << "}\n";
+      << "\"flops\"" << s1 << flops << s2
+      << "\"pairs_per_s\"" << s1 << extra.pairs_per_s;
+  if (extra.checked)
+    out << s2 << "\"check_targets\"" << s1 << extra.check_targets << s2
+        << "\"rel_l2\"" << s1 << extra.rel_l2 << s2
+        << "\"max_phase_err\"" << s1 << extra.max_phase_err;
+  out << "}\n";
   return out.str();
 }
 
 bool write_arrays(const std::vector<double> &amp, const std::vector<double> &phase,
                   const std::vector<double> &pos, const std::string &k1, const std::string &k2,
-                  const Plane &p, double dt, double flops, const std::string &dir,
-                  std::string *err) {
+                  const Plane &p, double dt, double flops, const Extra &extra,
+                  const std::string &dir, std::string *err) {
   static bool overwrite = true;  // the first call of the process truncates out.json
   struct timespec t;
   clock_gettime(CLOCK_MONOTONIC, &t);
-  const std::string line = metadata_line(k1, k2, p, amp, phase, dt, flops, (long)t.tv_nsec);
+  const std::string line = metadata_line(k1, k2, p, amp, phase, dt, flops, (long)t.tv_nsec, extra);
   FILE *f = fopen((dir + "out.json").c_str(), overwrite ? "wb" : "ab");
   if (!f) {
     *err = "cannot write " + dir + "out.json";

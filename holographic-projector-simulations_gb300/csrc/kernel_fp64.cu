@@ -27,8 +27,11 @@ struct Fp64Smem {
   static constexpr size_t bytes = bar + 2 * sizeof(uint64_t);
 };
 
-template <int THREADS, int R, int CS, bool CONST>
-__global__ void __launch_bounds__(THREADS)
+// MINB: CTAs per SM the register allocation must leave room for (the FP64 pipe
+// needs enough resident warps to hide the latency of its MUFU-seeded sqrt,
+// division and sin/cos sequences).
+template <int THREADS, int R, int CS, int MINB, bool CONST>
+__global__ void __launch_bounds__(THREADS, MINB)
     k_fp64(const Fp64Problem P, int n_items, int *err) {
   extern __shared__ __align__(128) unsigned char smem[];
   using L = Fp64Smem<THREADS, R, CS>;
@@ -129,31 +132,33 @@ constexpr Variant kVariants[] = {
     {256, 2, 256},  // 1
     {128, 2, 256},  // 2
     {64, 4, 256},   // 3
+    {128, 2, 256},  // 4: registers for 8 CTAs per SM
+    {128, 1, 256},  // 5: registers for 12 CTAs per SM
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-template <int THREADS, int R, int CS>
+template <int THREADS, int R, int CS, int MINB>
 int launch_variant(const Fp64Problem &p, int grid, bool cst, int *err, cudaStream_t s) {
   using L = Fp64Smem<THREADS, R, CS>;
   const int n_items = p.n_ttiles * p.splits;
   if (n_items <= 0) return HOLO_OK;
   if (cst) {
-    auto kern = k_fp64<THREADS, R, CS, true>;
-    HOLO_TRY((kernel_setup<k_fp64<THREADS, R, CS, true>>(THREADS, (int)L::bytes, nullptr)));
+    auto kern = k_fp64<THREADS, R, CS, MINB, true>;
+    HOLO_TRY((kernel_setup<k_fp64<THREADS, R, CS, MINB, true>>(THREADS, (int)L::bytes, nullptr)));
     kern<<<grid, THREADS, L::bytes, s>>>(p, n_items, err); note_launches(1);
   } else {
-    auto kern = k_fp64<THREADS, R, CS, false>;
-    HOLO_TRY((kernel_setup<k_fp64<THREADS, R, CS, false>>(THREADS, (int)L::bytes, nullptr)));
+    auto kern = k_fp64<THREADS, R, CS, MINB, false>;
+    HOLO_TRY((kernel_setup<k_fp64<THREADS, R, CS, MINB, false>>(THREADS, (int)L::bytes, nullptr)));
     kern<<<grid, THREADS, L::bytes, s>>>(p, n_items, err); note_launches(1);
   }
   HOLO_CUDA(cudaGetLastError());
   return HOLO_OK;
 }
 
-template <int THREADS, int R, int CS>
+template <int THREADS, int R, int CS, int MINB>
 int occupancy_variant(int *out) {
   using L = Fp64Smem<THREADS, R, CS>;
-  return kernel_setup<k_fp64<THREADS, R, CS, false>>(THREADS, (int)L::bytes, out);
+  return kernel_setup<k_fp64<THREADS, R, CS, MINB, false>>(THREADS, (int)L::bytes, out);
 }
 
 }  // namespace
@@ -163,22 +168,24 @@ Variant fp64_variant(int i) { return kVariants[i]; }
 
 #define HOLO_FP64_DISPATCH(V, CALL)                                        \
   switch (V) {                                                             \
-    case 0: return CALL(128, 4, 256);                                      \
-    case 1: return CALL(256, 2, 256);                                      \
-    case 2: return CALL(128, 2, 256);                                      \
-    case 3: return CALL(64, 4, 256);                                       \
+    case 0: return CALL(128, 4, 256, 1);                                   \
+    case 1: return CALL(256, 2, 256, 1);                                   \
+    case 2: return CALL(128, 2, 256, 1);                                   \
+    case 3: return CALL(64, 4, 256, 1);                                    \
+    case 4: return CALL(128, 2, 256, 8);                                   \
+    case 5: return CALL(128, 1, 256, 12);                                  \
     default: return fail(HOLO_ERR_INVALID, "unknown fp64 variant %d", V);  \
   }
 
 int launch_fp64(const Fp64Problem &p, int variant, int grid, bool const_phase, int *err,
                 cudaStream_t s) {
-#define CALL(T, R, C) launch_variant<T, R, C>(p, grid, const_phase, err, s)
+#define CALL(T, R, C, B) launch_variant<T, R, C, B>(p, grid, const_phase, err, s)
   HOLO_FP64_DISPATCH(variant, CALL)
 #undef CALL
 }
 
 int fp64_occupancy(int variant, int *ctas_per_sm) {
-#define CALL(T, R, C) occupancy_variant<T, R, C>(ctas_per_sm)
+#define CALL(T, R, C, B) occupancy_variant<T, R, C, B>(ctas_per_sm)
   HOLO_FP64_DISPATCH(variant, CALL)
 #undef CALL
 }

@@ -19,7 +19,9 @@
 //   - all calls on a device share the array and each call overwrites it: two
 //     calls that overlap on the GPU would race.  Calls in this process are
 //     serialised by a lock and each call returns only after its work on
-//     `stream` has finished;
+//     `stream` has finished -- on failure too, once anything was queued;
+//   - input and output pointers must be memory of `device` (or managed
+//     memory): the path enables no peer access;
 //   - the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current); make that first call
 //     before any stream capture.
@@ -140,14 +142,29 @@ void model_from_stats(const double *st, double *base, double *curv, double *lin,
   split_error_model(t, base, curv, lin, gemm);
 }
 
-bool is_device_pointer(const void *p) {
+// Memory the kernels on `device` may read and write: device memory of that GPU
+// (memory of another GPU would need peer access, which this path never enables)
+// or managed memory.
+bool is_device_pointer(const void *p, int device) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == device;
 }
+
+// Once work is queued on the stream, every return -- the failure paths included
+// -- waits for it: the scratch array is shared, and the next call (let in by the
+// lock as soon as this one returns) overwrites it.
+struct DrainOnReturn {
+  cudaStream_t s;
+  bool armed = false;
+  ~DrainOnReturn() {
+    if (armed) cudaStreamSynchronize(s);  // its status: already reported by the failing call
+  }
+};
 
 int transform_noalloc(int device, int sign, double lambda, const double *amp,
                       const double *phase, const double *u, size_t N, const double *v,
@@ -158,15 +175,20 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
     return fail(HOLO_ERR_INVALID, "null input or output array");
   for (const void *p : {(const void *)amp, (const void *)phase, (const void *)u, (const void *)v,
                         (const void *)y})
-    if (p && !is_device_pointer(p))
-      return fail(HOLO_ERR_INVALID, "holo_transform_noalloc takes device pointers only");
+    if (p && !is_device_pointer(p, device))
+      return fail(HOLO_ERR_INVALID,
+                  "holo_transform_noalloc takes device pointers of device %d (or managed "
+                  "memory) only",
+                  device);
   const size_t lim = (size_t)kSortBlock * 4096;
   if (N > lim || M > lim) return fail(HOLO_ERR_INVALID, "point count above the supported %zu", lim);
   if (M == 0) return HOLO_OK;
 
   unsigned char *base = nullptr;
   HOLO_TRY(noalloc_scratch(device, &base));
+  DrainOnReturn drain{s};  // armed at the first work queued on `s`
   if (N == 0) {
+    drain.armed = true;
     HOLO_CUDA(cudaMemsetAsync(y, 0, M * sizeof(double2), s));
     HOLO_CUDA(cudaStreamSynchronize(s));
     return HOLO_OK;
@@ -203,6 +225,7 @@ int transform_noalloc(int device, int sign, double lambda, const double *amp,
                 "problem needs %zu bytes of the %zu-byte no-alloc scratch (N=%zu, M=%zu)",
                 std::max(need, shared_off + partial_min), kNoAllocBytes, N, M);
 
+  drain.armed = true;
   HOLO_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));  // the error word starts at zero
   // ---- tile order of both point sets ----
   HOLO_TRY(tile_order(u, (int)N, order_s, ts, s, kTileHilbert));

@@ -84,6 +84,25 @@ __global__ void __launch_bounds__(256) k_probe_ffma2(float *out, int iters, floa
   if (s == 12345.f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// FP64 FMA chains: the rate of the DFMA pipe, the denominator of the plain FP64
+// kernel's roofline (every FP64 operation of a pair issues on that pipe).  16
+// independent chains per thread: a warp's DFMA holds the pipe for many cycles,
+// so the probe needs more operations in flight than the FP32 ones.
+__global__ void __launch_bounds__(256) k_probe_dfma(float *out, int iters, float seed) {
+  double x[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) x[j] = (double)seed + 0.001 * (threadIdx.x + j);
+  const double a = 0.999, b = 0.0001;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) x[j] = fma(x[j], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) s += x[j];
+  if (s == 12345.0) out[blockIdx.x * blockDim.x + threadIdx.x] = (float)s;
+}
+
 // One thread waits, bounded, on a barrier phase that nothing completes: the
 // timeout path of every pipelined kernel here (raise the error word, return).
 __global__ void k_selftest_wait(long long max_cycles, int *err) {
@@ -154,16 +173,16 @@ int holo_selftest_bounded_wait(holo_handle h, long long max_cycles, holo_stream_
 
 // kind 0: MUFU sin.approx.f32 ops/s, kind 1: FP32 FMA ops/s (one op = one
 // lane-instruction), kind 2: packed fma.rn.f32x2 lane-instructions/s (each is
-// two FMAs)
+// two FMAs), kind 3: FP64 FMA ops/s
 int holo_probe_peak(holo_handle h, int kind, double *ops_per_s) {
   if (!h || !ops_per_s) return fail(HOLO_ERR_INVALID, "null argument");
-  if (kind < 0 || kind > 2) return fail(HOLO_ERR_INVALID, "unknown probe %d", kind);
+  if (kind < 0 || kind > 3) return fail(HOLO_ERR_INVALID, "unknown probe %d", kind);
   std::lock_guard<std::mutex> lk(h->mu);
   int prev = -1;
   cudaGetDevice(&prev);
   cudaSetDevice(h->device);
   const int blocks = h->sm_count * 8, threads = 256;
-  const int iters = kind == 0 ? 4096 : 32768;
+  const int iters = kind == 0 ? 4096 : kind == 3 ? 512 : 32768;
   float *out = nullptr;
   HOLO_CUDA(cudaMalloc(&out, (size_t)blocks * threads * sizeof(float)));
   cudaEvent_t e0, e1;
@@ -174,12 +193,13 @@ int holo_probe_peak(holo_handle h, int kind, double *ops_per_s) {
     cudaEventRecord(e0);
     if (kind == 0) k_probe_mufu<<<blocks, threads>>>(out, iters, 0.1f + rep);
     else if (kind == 1) k_probe_ffma<<<blocks, threads>>>(out, iters, 0.1f + rep);
-    else k_probe_ffma2<<<blocks, threads>>>(out, iters, 0.1f + rep);
+    else if (kind == 2) k_probe_ffma2<<<blocks, threads>>>(out, iters, 0.1f + rep);
+    else k_probe_dfma<<<blocks, threads>>>(out, iters, 0.1f + rep);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    const double ops = (double)blocks * threads * iters * 8.0;
+    const double ops = (double)blocks * threads * iters * (kind == 3 ? 16.0 : 8.0);
     if (rep > 0 && ms > 0) best = std::max(best, ops / (ms * 1e-3));
   }
   cudaEventDestroy(e0);

@@ -249,7 +249,8 @@ int holo_autotune(holo_handle h, int precision, size_t N, size_t M, int repeats,
  * launched on the handle in between (end synchronises those events).
  * holo_probe_peak: measured issue rate of this GPU's pipes, kind 0 = MUFU
  * (sin.approx.f32, the XU pipe), kind 1 = FP32 FMA, kind 2 = packed FP32 pair
- * FMA (fma.rn.f32x2, two FMAs each), in lane-instructions per second. */
+ * FMA (fma.rn.f32x2, two FMAs each), kind 3 = FP64 FMA (the FP64 pipe), in
+ * lane-instructions per second. */
 int holo_kernel_launches(long long *out);
 int holo_profile_begin(holo_handle h);
 int holo_profile_end(holo_handle h, double *total_ms, int *launches);

@@ -8,6 +8,10 @@
  * (the hook at cuda/macros.h:44-46).  LAMBDA is a compile-time macro in the
  * reference (cuda/macros.h:23-25), so the Makefile builds one probe per
  * wavelength.  Used only to pin the C oracle and to write golden fixtures.
+ * It also wraps the reference's host-side data generators, init::plane (the
+ * projector / projection lattice without -r, cuda/init.h:89-158) and
+ * init::sparse_plane (the object shapes, cuda/init.h:160-234), whose outputs pin
+ * the device generators of the holo CLI.
  */
 #include <cuComplex.h>
 #include <curand.h>
@@ -35,6 +39,7 @@ struct ProbeBlockReduce {
 #include "main.h"
 #include "kernel.cu"
 #include "superposition.cu"
+#include "init.h"
 
 extern "C" {
 
@@ -68,6 +73,29 @@ void ref_transform(size_t N, const double *amp, const double *phase, const doubl
     y[2 * m] = acc.x;
     y[2 * m + 1] = acc.y;
   }
+}
+
+/* init::plane without -r (no CUDA call is made then): n points, xyz-interleaved. */
+void ref_plane(size_t n, double width, double ox, double oy, double oz, double aspect,
+               double *out) {
+  std::vector<SPACE> v(n * DIMS, 0.0);
+  Plane p;
+  p.width = width;
+  p.offset = {ox, oy, oz};
+  p.aspect_ratio = aspect;
+  p.randomize = false;
+  init::plane(v, p);
+  for (size_t i = 0; i < n * DIMS; ++i) out[i] = v[i];
+}
+
+/* init::sparse_plane on `inout` (n points, xyz-interleaved; entries the shape leaves
+ * alone keep their values).  shape: 0 Line, 1 LogLine, 2 Circle, 3 DottedCircle. */
+void ref_sparse_plane(size_t n, int shape, double width, double ox, double oy, double oz,
+                      double modulate, double *inout) {
+  std::vector<SPACE> u(inout, inout + n * DIMS);
+  const Cartesian<double> off = {ox, oy, oz};
+  init::sparse_plane(u, static_cast<Shape>(shape), width, off, modulate);
+  for (size_t i = 0; i < n * DIMS; ++i) inout[i] = u[i];
 }
 
 }  // extern "C"

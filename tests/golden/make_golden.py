@@ -19,9 +19,16 @@ Fixtures
   transform_small.npz             x->y (Backwards) and y->z (Forwards) sums of the
                                   reference's own terms on a small grid, plus the
                                   prototype's polar output for the same x->y sum
+  generators.npz                  the reference's own init::plane lattices (without
+                                  -r) and init::sparse_plane object shapes for the
+                                  planes of the holo CLI runs in
+                                  tests/test_gpu_generators.py
+
+``python make_golden.py generators`` writes generators.npz alone.
 """
 from __future__ import annotations
 
+import ctypes
 import json
 import os
 import subprocess
@@ -65,6 +72,59 @@ def grid(nx: int, ny: int, pitch: float, z: float) -> np.ndarray:
     ys = (np.arange(ny) - (ny - 1) / 2.0) * pitch
     X, Y = np.meshgrid(xs, ys, indexing="ij")
     return np.stack([X.ravel(), Y.ravel(), np.full(nx * ny, z)], axis=1)
+
+
+# Planes of the generated-mode runs in tests/test_gpu_generators.py (holo -x 16 -y 4096
+# -z 1024 -a 1.5 -A 0.8 -l 3e-3 -n 1.2e-3 -o 2e-4 -O 4e-4 -u 1e-4 -U 3e-4 -v -2e-4 -w 0.3
+# -X 2 --shape S): per object plane i (ratio i), the object's width and offset, the
+# projector lattice and the projection lattice, as the reference derives them
+# (cuda/main.cu:125-181: lerp of the ranges, gerp of z; z offset fixed here).
+GEN_PLANES = [
+    # (object width, object offset xyz, modulate)
+    (2e-4, (1e-4, -2e-4, 0.3), 0.0),
+    (4e-4, (3e-4, -2e-4, 0.3), 0.5),
+]
+GEN_SHAPES = {"line": 0, "log-line": 1, "circle": 2, "dotted-circle": 3}
+
+
+def generators() -> None:
+    """The reference's own generators through the probe (host code: no GPU needed)."""
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "all", f"REF={REF}"],
+                   check=True)
+    R = oracle.reference_probe("650")
+    assert R is not None
+    dp = oracle._dp
+    R.ref_plane.restype = None
+    R.ref_plane.argtypes = [ctypes.c_size_t] + [ctypes.c_double] * 5 + [dp]
+    R.ref_sparse_plane.restype = None
+    R.ref_sparse_plane.argtypes = [ctypes.c_size_t, ctypes.c_int] + [ctypes.c_double] * 5 + [dp]
+
+    def plane(n, width, off, aspect):
+        out = np.zeros(3 * n)
+        R.ref_plane(n, width, off[0], off[1], off[2], aspect, out.ctypes.data_as(dp))
+        return out
+
+    out = {}
+    # the projector (-y 4096 -a 1.5 -l 3e-3, at the origin) and the projection plane
+    # (-z 1024 -A 0.8 -n 1.2e-3, at the object's offset) of each object plane
+    for i, (_, off, _) in enumerate(GEN_PLANES):
+        out[f"v{i}"] = plane(4096, 3e-3, (0.0, 0.0, 0.0), 1.5)
+        out[f"w{i}_0"] = plane(1024, 1.2e-3, off, 0.8)
+    # the default projector of a plain run (-y 4096, width 512 x 7 um, square)
+    out["v_default"] = plane(4096, 512 * 7e-6, (0.0, 0.0, 0.0), 1.0)
+    # object shapes: 16 points, the array carried from plane to plane as the CLI does
+    for name, code in GEN_SHAPES.items():
+        u = np.zeros(3 * 16)
+        for i, (width, off, mod) in enumerate(GEN_PLANES):
+            R.ref_sparse_plane(16, code, width, off[0], off[1], off[2], mod,
+                               u.ctypes.data_as(dp))
+            out[f"u{i}_{name}"] = u.copy()
+    # one point (the n == 1 branch)
+    u1 = np.zeros(3)
+    R.ref_sparse_plane(1, 2, 2e-4, 1e-4, -2e-4, 0.3, 0.0, u1.ctypes.data_as(dp))
+    out["u_single"] = u1
+    np.savez_compressed(os.path.join(HERE, "generators.npz"), **out)
+    print("generators.npz written to", HERE)
 
 
 def main() -> None:
@@ -150,4 +210,8 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["generators"]:
+        generators()
+    else:
+        main()
+        generators()

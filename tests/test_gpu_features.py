@@ -223,6 +223,39 @@ def test_cli_file_mode_chain(holo, orc, tmp_path):
         assert k in meta[0]
 
 
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("split32", 1e-5)])
+def test_cli_check_writes_accuracy_keys(holo, orc, tmp_path, prec, tol):
+    """--check K: every pass compared with the FP64 sum at K targets; out.json carries
+    pairs_per_s on every line and check_targets / rel_l2 / max_phase_err after the
+    reference's keys (cuda/util.h:358-396).  The reported y-pass error is checked here
+    against the oracle at the same targets."""
+    rng = np.random.default_rng(23)
+    u = grid(32, 10e-6, 0.35)
+    v = grid(128, 7.56e-6, 0.0)
+    w = grid(32, 10e-6, 0.35)
+    amp, phase = rng.uniform(0, 1, len(u)), rng.uniform(0, 2 * np.pi, len(u))
+    holo.io.write_inputs(str(tmp_path), amp, phase, u, v, w)
+    r = subprocess.run([_cli(holo), "-f", str(tmp_path), "-F", "--lambda", str(LAM),
+                        "--precision", prec, "--check", "300"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    meta = holo.io.parse_out_json(str(tmp_path / "out.json"))
+    assert [m["phasor"] for m in meta] == ["y0", "z0_0"]
+    for m in meta:
+        assert m["pairs_per_s"] > 0 and m["check_targets"] == 300
+        assert 0 <= m["rel_l2"] < tol and 0 <= m["max_phase_err"] < 1e3 * tol
+    # the y line's error, recomputed: the file field scaled back by max |y| against the oracle
+    M, K = len(v), 300
+    idx = ((np.arange(K) + 0.5) * M / K).astype(np.int64)
+    exact = orc.transform_subset(amp, phase, u, v, idx, -1, LAM)
+    ya = holo.io.read_dat(str(tmp_path / "y0_amp.dat"))
+    yp = holo.io.read_dat(str(tmp_path / "y0_phase.dat"))
+    scale = np.abs(orc.transform(amp, phase, u, v, -1, LAM)).max()
+    got = ya[idx] * scale * np.exp(1j * yp[idx])
+    assert rel_l2(got, exact) < tol
+    if prec == "fp64":  # same scale as the CLI's to ~1e-16: the two figures agree
+        assert meta[0]["rel_l2"] == pytest.approx(rel_l2(got, exact), abs=1e-13)
+
+
 def test_cli_ref_compat_and_w0_fallback(holo, orc, tmp_path):
     rng = np.random.default_rng(22)
     u = grid(8, 10e-6, 0.35)
