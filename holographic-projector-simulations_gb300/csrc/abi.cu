@@ -1123,6 +1123,8 @@ int holo_variant_describe(int precision, int variant, int *threads, int *targets
   if (n < 0) return n;
   if (variant < 0 || variant >= n) return fail(HOLO_ERR_INVALID, "variant %d out of range", variant);
   const Variant V = precision == HOLO_SPLIT32 ? split_variant(variant) : fp64_variant(variant);
+  if (V.tc && !split_tc_has_build(V.cs, V.poly, V.sc))
+    return fail(HOLO_ERR_INVALID, "split variant %d names no tensor-core kernel build", variant);
   if (threads) *threads = V.threads;
   if (targets_per_thread) *targets_per_thread = V.r;
   if (source_tile) *source_tile = V.cs;

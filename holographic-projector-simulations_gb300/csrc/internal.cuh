@@ -70,7 +70,8 @@ struct Variant {
   int packed = 0; // 1: pair loop on packed FP32 pairs (two sources per instruction)
   int ws = 0;     // 1: warp-specialised sin/cos (`poly` is then the average per thread)
   int tc = 0;     // 1: phase on the tensor cores (kernel_tc.cu; `poly` of 16 source pairs)
-  int sc = 0;     // tc only: MUFU pairs accumulated in scalar FP32
+  int sc = 0;     // tc only, build flags: 1 MUFU pairs accumulated in scalar FP32, 4 chunk
+                 // loop half unrolled, 8 one reciprocal for the target row's 1/Qt, 1/Qt^2
   int tt() const { return threads * r; }
 };
 
@@ -214,12 +215,15 @@ int launch_gather_apf(const double *amp, const double *phase, const int32_t *ord
 // kernel_tc.cu: the tensor-core split kernel (pair model 3) on source tiles of `cs`
 // (1024, 512 or 256: 4 consumer warps per TMEM lane group and MMA blocks of 256
 // sources; 768: 6 consumer warps, blocks of 192), `poly16` of every 16 source pairs
-// on the FMA-pipe sin/cos, `scalar`: MUFU pairs accumulated unpacked
-int launch_split_tc(const SplitProblem &p, int cs, int poly16, bool scalar, int grid, int *err,
+// on the FMA-pipe sin/cos, `flags` (Variant.sc): 1 MUFU pairs accumulated unpacked, 4
+// chunk loop half unrolled, 8 one reciprocal for the target row's 1/Qt and 1/Qt^2
+int launch_split_tc(const SplitProblem &p, int cs, int poly16, int flags, int grid, int *err,
                     cudaStream_t s);
-int split_tc_occupancy(int cs, int poly16, bool scalar, int *ctas_per_sm);
+int split_tc_occupancy(int cs, int poly16, int flags, int *ctas_per_sm);
+// Whether a tensor-core build exists for (cs, poly16, flags) (host only, no CUDA call).
+bool split_tc_has_build(int cs, int poly16, int flags);
 int launch_split_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items,
-                            int *queue, int cs, int poly16, bool scalar, int grid, int *err,
+                            int *queue, int cs, int poly16, int flags, int grid, int *err,
                             cudaStream_t s);
 int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase, bool mc,
                  int *err, cudaStream_t s);

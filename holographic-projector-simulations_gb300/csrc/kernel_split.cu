@@ -519,6 +519,12 @@ constexpr Variant kVariants[] = {
     {512, 1, 512, 6, 3, 1, 0, 1},      // 44
     {512, 1, 256, 6, 3, 1, 0, 1},      // 45
     {128, 4, 256, 1, 2, 1},            // 46: packed model 2, TT 512 x source tiles of 256
+    // pair model 3, build flags 4 (chunk loop half unrolled) and 8 (one reciprocal for
+    // the target row's 1/Qt and 1/Qt^2)
+    {512, 1, 1024, 6, 3, 1, 0, 1, 4},   // 47: as 34
+    {512, 1, 1024, 6, 3, 1, 0, 1, 8},   // 48: as 34
+    {512, 1, 1024, 6, 3, 1, 0, 1, 12},  // 49: as 34
+    {512, 1, 1024, 7, 3, 1, 0, 1, 4},   // 50: as 36
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -636,7 +642,7 @@ int launch_split(const SplitProblem &p, int variant, int grid, bool const_phase,
   if (is_tc(variant)) {
     if (!const_phase && !mc)
       return launch_split_tc(p, kVariants[variant].cs, kVariants[variant].poly,
-                             kVariants[variant].sc != 0, grid, err, s);
+                             kVariants[variant].sc, grid, err, s);
     variant = tc_fallback(variant);
   }
 #define CALL(T, R, C, P) launch_variant<T, R, C, P>(p, grid, const_phase, mc, err, s)
@@ -648,7 +654,7 @@ int launch_split_batched(const SplitProblem *probs_dev, const WorkItem *items, i
                          int *queue, int variant, int grid, int *err, cudaStream_t s) {
   if (is_tc(variant))
     return launch_split_tc_batched(probs_dev, items, n_items, queue, kVariants[variant].cs,
-                                   kVariants[variant].poly, kVariants[variant].sc != 0, grid, err,
+                                   kVariants[variant].poly, kVariants[variant].sc, grid, err,
                                    s);
 #define CALL(T, R, C, P) batched_variant<T, R, C, P>(probs_dev, items, n_items, queue, grid, err, s)
   HOLO_SPLIT_DISPATCH(variant, CALL)
@@ -659,7 +665,7 @@ int split_occupancy(int variant, bool mc, int *ctas_per_sm) {
   if (is_tc(variant)) {
     if (!mc)
       return split_tc_occupancy(kVariants[variant].cs, kVariants[variant].poly,
-                                kVariants[variant].sc != 0, ctas_per_sm);
+                                kVariants[variant].sc, ctas_per_sm);
     variant = tc_fallback(variant);
   }
 #define CALL(T, R, C, P) occupancy_variant<T, R, C, P>(mc, ctas_per_sm)

@@ -38,6 +38,8 @@
 // after a timeout the kernel raises the device error word and skips the rest
 // of its work, then waits (bounded) for the MMAs it issued and frees the
 // tensor memory.
+#include <type_traits>
+
 #include "internal.cuh"
 #include "ptx.cuh"
 
@@ -143,10 +145,16 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
   return false;
 }
 
+// Build flags: kTcScalar -- the MUFU pairs accumulated in scalar FP32 (no packing);
+// kTcHalfUnroll -- the 16-column chunks of a block in a loop of chunk pairs instead
+// of fully unrolled (half the pair-loop code); kTcRcp -- the target row's 1/Qt and
+// 1/Qt^2 from one correctly rounded reciprocal instead of two divisions.
+constexpr int kTcScalar = 1, kTcHalfUnroll = 4, kTcRcp = 8;
+
 // BATCHED: work items (problem, target tile, source range, split) come from a
 // device queue (atomic counter) and each names its own problem descriptor;
 // otherwise item i of problem P0 is target tile i / splits, split i % splits.
-template <int CG, int NBLK, int NPP0, int NPP1, bool SC, bool BATCHED>
+template <int CG, int NBLK, int NPP0, int NPP1, int FL, bool BATCHED>
 __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
     k_split_tc(const SplitProblem P0, const SplitProblem *__restrict__ probs,
                const WorkItem *__restrict__ items, int n_items, int *queue, int *err) {
@@ -338,7 +346,15 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
           const float Ty = fmaf(f2x, th[0], fmaf(f2y, th[1], f2z * th[2]));
           const float Qt = fr->r0f + fmaf(fex, th[0], fmaf(fey, th[1], fez * th[2]));
           const float T2 = fmaf(Tx, Tx, Ty * Ty);
-          const float Iq = ak / Qt, Kq = Iq / Qt;
+          float Iq, Kq;
+          if (FL & kTcRcp) {
+            const float rq = __frcp_rn(Qt);
+            Iq = ak * rq;
+            Kq = Iq * rq;
+          } else {
+            Iq = ak / Qt;
+            Kq = Iq / Qt;
+          }
           f[0] = Iq; f[1] = -2.f * Iq * Tx; f[2] = -2.f * Iq * Ty; f[3] = Kq * T2;
           f[4] = Kq; f[5] = -2.f * Kq * Tx; f[6] = -2.f * Kq * Ty; f[7] = 0.f;
           tph_v = B + sgn * Iq * T2;  // the target's rotation, incl. the Iq T2 term
@@ -457,10 +473,12 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
               uint32_t rv[2][16];
               ptx::tmem_ld16_nowait(ta, rv[0]);
               ptx::tmem_wait16(rv[0]);
-#pragma unroll
-              for (int ch = 0; ch < S::Chunks; ++ch) {
+              // chunk ch (parity P = ch & 1, a compile-time constant): its phases are in
+              // rv[P]; the load of chunk ch + 1 into rv[P ^ 1] is in flight meanwhile
+              auto chunk = [&](auto parity, const int ch) {
+                constexpr int P = decltype(parity)::value;
                 if (ch + 1 < S::Chunks)
-                  ptx::tmem_ld16_nowait(ta + (uint32_t)(16 * (ch + 1)), rv[(ch + 1) & 1]);
+                  ptx::tmem_ld16_nowait(ta + (uint32_t)(16 * (ch + 1)), rv[P ^ 1]);
                 const float4 *ap =
                     reinterpret_cast<const float4 *>(amp + (j & 1) * kTcCS + n * kTcN +
                                                      cg * S::Cols + 16 * ch);
@@ -473,13 +491,13 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
                   av[4 * q + 2] = v.z;
                   av[4 * q + 3] = v.w;
                 }
-                const uint32_t *th = rv[ch & 1];
-                const int npp = (ch & 1) ? NPP1 : NPP0;
+                const uint32_t *th = rv[P];
+                constexpr int npp = P ? NPP1 : NPP0;
 #pragma unroll
                 for (int pp = 0; pp < 8; ++pp) {
                   const float t0 = __uint_as_float(th[2 * pp]);
                   const float t1 = __uint_as_float(th[2 * pp + 1]);
-                  if (SC && pp >= npp) {
+                  if ((FL & kTcScalar) && pp >= npp) {
                     // XU pipe, scalar accumulation (no packing of the MUFU results)
                     res[0] = fmaf(av[2 * pp], ptx::cos_approx(t0), res[0]);
                     ims[0] = fmaf(av[2 * pp], ptx::sin_approx(t0), ims[0]);
@@ -501,7 +519,23 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
                   re2 = ptx::fma2(am, cs, re2);
                   im2 = ptx::fma2(am, sn, im2);
                 }
-                if (ch + 1 < S::Chunks) ptx::tmem_wait16(rv[(ch + 1) & 1]);
+                if (ch + 1 < S::Chunks) ptx::tmem_wait16(rv[P ^ 1]);
+              };
+              static_assert(S::Chunks % 2 == 0, "chunks come in pairs");
+              using Even = std::integral_constant<int, 0>;
+              using Odd = std::integral_constant<int, 1>;
+              if (FL & kTcHalfUnroll) {
+#pragma unroll 1
+                for (int ch = 0; ch < S::Chunks; ch += 2) {
+                  chunk(Even{}, ch);
+                  chunk(Odd{}, ch + 1);
+                }
+              } else {
+#pragma unroll
+                for (int ch = 0; ch < S::Chunks; ch += 2) {
+                  chunk(Even{}, ch);
+                  chunk(Odd{}, ch + 1);
+                }
               }
             }
             ptx::tc_fence_before();
@@ -545,12 +579,12 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
   if (producer) ptx::tmem_dealloc(tbase, kTcCols);
 }
 
-template <int CG, int NBLK, int NPP0, int NPP1, bool SC>
+template <int CG, int NBLK, int NPP0, int NPP1, int FL>
 int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
-  auto kern = k_split_tc<CG, NBLK, NPP0, NPP1, SC, false>;
+  auto kern = k_split_tc<CG, NBLK, NPP0, NPP1, FL, false>;
   constexpr int bytes = (int)TcSmem<CG, NBLK>::bytes;
   constexpr int threads = TcShape<CG, NBLK>::Threads;
-  HOLO_TRY((kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, SC, false>>(threads, bytes, nullptr)));
+  HOLO_TRY((kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, FL, false>>(threads, bytes, nullptr)));
   const int n_items = p.n_ttiles * p.splits;
   if (n_items <= 0) return HOLO_OK;
   kern<<<grid, threads, bytes, s>>>(p, nullptr, nullptr, n_items, nullptr, err);
@@ -559,69 +593,91 @@ int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
   return HOLO_OK;
 }
 
-template <int CG, int NBLK, int NPP0, int NPP1, bool SC>
+template <int CG, int NBLK, int NPP0, int NPP1, int FL>
 int launch_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items, int *queue,
                       int grid, int *err, cudaStream_t s) {
-  auto kern = k_split_tc<CG, NBLK, NPP0, NPP1, SC, true>;
+  auto kern = k_split_tc<CG, NBLK, NPP0, NPP1, FL, true>;
   constexpr int bytes = (int)TcSmem<CG, NBLK>::bytes;
   constexpr int threads = TcShape<CG, NBLK>::Threads;
-  HOLO_TRY((kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, SC, true>>(threads, bytes, nullptr)));
+  HOLO_TRY((kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, FL, true>>(threads, bytes, nullptr)));
   kern<<<grid, threads, bytes, s>>>(SplitProblem{}, probs, items, n_items, queue, err);
   note_launches(1);
   HOLO_CUDA(cudaGetLastError());
   return HOLO_OK;
 }
 
-template <int CG, int NBLK, int NPP0, int NPP1, bool SC>
+template <int CG, int NBLK, int NPP0, int NPP1, int FL>
 int occupancy_tc(int *out) {
   constexpr int bytes = (int)TcSmem<CG, NBLK>::bytes;
-  return kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, SC, false>>(TcShape<CG, NBLK>::Threads,
+  return kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, FL, false>>(TcShape<CG, NBLK>::Threads,
                                                                    bytes, out);
 }
 
-// builds: source tile, polynomial pairs per 16 (even chunk + odd chunk), scalar MUFU
-// accumulation
-#define HOLO_TC_DISPATCH(CS, NP16, SCAL, CALL)                                            \
-  switch ((CS) * 100 + (NP16) * 2 + ((SCAL) ? 1 : 0)) {                                   \
-    case 102408: return CALL(4, 4, 2, 2, false);                                          \
-    case 102410: return CALL(4, 4, 2, 3, false);                                          \
-    case 102412: return CALL(4, 4, 3, 3, false);                                          \
-    case 102413: return CALL(4, 4, 3, 3, true);                                           \
-    case 102414: return CALL(4, 4, 3, 4, false);                                          \
-    case 102415: return CALL(4, 4, 3, 4, true);                                           \
-    case 102416: return CALL(4, 4, 4, 4, false);                                          \
-    case 51212: return CALL(4, 2, 3, 3, false);                                           \
-    case 25612: return CALL(4, 1, 3, 3, false);                                           \
-    case 76810: return CALL(6, 4, 2, 3, false);                                           \
-    case 76812: return CALL(6, 4, 3, 3, false);                                           \
-    case 76814: return CALL(6, 4, 3, 4, false);                                           \
+// builds: source tile CS, polynomial pairs A of even and B of odd chunks (A + B of every
+// 16 source pairs), build flags (kTcScalar, kTcHalfUnroll, kTcRcp).  The key and the template
+// arguments come from the same four numbers: 768-source tiles are 4 blocks of 192 with
+// 6 column groups, the others CS / 256 blocks of 256 with 4.  A use site defines
+// CALL(CG, NBLK, A, B, FL) and expands HOLO_TC_SWITCH.
+#define HOLO_TC_KEY(CS, NP16, FLAGS) ((CS) * 1000 + (NP16) * 10 + (FLAGS))
+#define HOLO_TC_CASE(CS, A, B, FL)     \
+  case HOLO_TC_KEY(CS, (A) + (B), FL): \
+    return CALL(((CS) == 768 ? 6 : 4), ((CS) == 768 ? 4 : (CS) / 256), A, B, FL);
+#define HOLO_TC_BUILDS                        \
+  HOLO_TC_CASE(1024, 2, 2, 0)                 \
+  HOLO_TC_CASE(1024, 2, 3, 0)                 \
+  HOLO_TC_CASE(1024, 3, 3, 0)                 \
+  HOLO_TC_CASE(1024, 3, 3, kTcScalar)         \
+  HOLO_TC_CASE(1024, 3, 3, kTcHalfUnroll)     \
+  HOLO_TC_CASE(1024, 3, 3, kTcRcp)            \
+  HOLO_TC_CASE(1024, 3, 3, kTcHalfUnroll | kTcRcp) \
+  HOLO_TC_CASE(1024, 3, 4, 0)                 \
+  HOLO_TC_CASE(1024, 3, 4, kTcScalar)         \
+  HOLO_TC_CASE(1024, 3, 4, kTcHalfUnroll)     \
+  HOLO_TC_CASE(1024, 4, 4, 0)                 \
+  HOLO_TC_CASE(512, 3, 3, 0)                  \
+  HOLO_TC_CASE(256, 3, 3, 0)                  \
+  HOLO_TC_CASE(768, 2, 3, 0)                  \
+  HOLO_TC_CASE(768, 3, 3, 0)                  \
+  HOLO_TC_CASE(768, 3, 4, 0)
+#define HOLO_TC_SWITCH(CS, NP16, FLAGS)                                                   \
+  switch (HOLO_TC_KEY(CS, NP16, FLAGS)) {                                                 \
+    HOLO_TC_BUILDS                                                                        \
     default:                                                                              \
       return fail(HOLO_ERR_INVALID,                                                       \
-                  "tensor-core split kernel: no build for source tiles of %d, %d of 16", CS, \
-                  NP16);                                                                  \
+                  "tensor-core split kernel: no build for source tiles of %d, %d of 16, "  \
+                  "flags %d", CS, NP16, FLAGS);                                           \
   }
 
 }  // namespace
 
-int launch_split_tc(const SplitProblem &p, int cs, int poly16, bool scalar, int grid, int *err,
+int launch_split_tc(const SplitProblem &p, int cs, int poly16, int flags, int grid, int *err,
                     cudaStream_t s) {
 #define CALL(G, NB, A, B, C) launch_tc<G, NB, A, B, C>(p, grid, err, s)
-  HOLO_TC_DISPATCH(cs, poly16, scalar, CALL)
+  HOLO_TC_SWITCH(cs, poly16, flags)
 #undef CALL
 }
 
 int launch_split_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items,
-                            int *queue, int cs, int poly16, bool scalar, int grid, int *err,
+                            int *queue, int cs, int poly16, int flags, int grid, int *err,
                             cudaStream_t s) {
 #define CALL(G, NB, A, B, C) \
   launch_tc_batched<G, NB, A, B, C>(probs, items, n_items, queue, grid, err, s)
-  HOLO_TC_DISPATCH(cs, poly16, scalar, CALL)
+  HOLO_TC_SWITCH(cs, poly16, flags)
 #undef CALL
 }
 
-int split_tc_occupancy(int cs, int poly16, bool scalar, int *ctas_per_sm) {
+int split_tc_occupancy(int cs, int poly16, int flags, int *ctas_per_sm) {
 #define CALL(G, NB, A, B, C) occupancy_tc<G, NB, A, B, C>(ctas_per_sm)
-  HOLO_TC_DISPATCH(cs, poly16, scalar, CALL)
+  HOLO_TC_SWITCH(cs, poly16, flags)
+#undef CALL
+}
+
+bool split_tc_has_build(int cs, int poly16, int flags) {
+#define CALL(G, NB, A, B, C) true
+  switch (HOLO_TC_KEY(cs, poly16, flags)) {
+    HOLO_TC_BUILDS
+    default: return false;
+  }
 #undef CALL
 }
 

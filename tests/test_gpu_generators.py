@@ -6,12 +6,15 @@ shapes, cuda/init.h:160-234), compiled here from its sources (oracle/ref_probe.c
 tests/golden/make_golden.py).  The holo CLI builds the same planes with device kernels
 (csrc/gen.cu); lattices and line objects must equal the reference bit for bit.  Shapes
 that call sin, cos, pow or log10 may differ in the last places (CUDA's math library
-against the C library): at most 2 ulps.
+against the C library): at most 2 ulps of the largest coordinate of the plane (an
+offset added to a sine can cancel leading digits, so ulps of the result itself would
+overstate the difference); their heights are exact.
 
 The -r jitter (cuda/init.h:19-34, 120-141) is compared bit for bit with cuRAND's XORWOW
-sequence drawn on the host (curandCreateGeneratorHost, seed 1235 for the first lattice),
-consumed the reference's way: per lattice row, x + y uniforms, then a discarded call of
-(x + y) / 8.
+device generator driven from the test (seed 1235 for the first lattice, 1236 for the
+next), called the reference's way: per lattice row, x + y uniforms into a buffer, then
+(x + y) / 8 more into the start of the same buffer, which the row then reads.  (cuRAND's
+host-side generator does not reproduce the device generator's sequence.)
 """
 import ctypes
 import ctypes.util
@@ -43,8 +46,10 @@ def _run(holo, out, *flags):
     return lambda name: holo.io.read_dat(str(out / f"{name}.dat"))
 
 
-def _ulps(a, b):
-    return np.max(np.abs(a - b) / np.spacing(np.maximum(np.abs(b), 1e-300)))
+def _xy_ulps(u, ref):
+    """Largest difference of the x, y coordinates in ulps of the plane's largest one."""
+    a, b = u.reshape(-1, 3)[:, :2], ref.reshape(-1, 3)[:, :2]
+    return float(np.max(np.abs(a - b)) / np.spacing(np.max(np.abs(b))))
 
 
 @pytest.mark.parametrize("shape", ["line", "log-line", "circle", "dotted-circle"])
@@ -60,7 +65,8 @@ def test_planes_match_the_reference_generators(holo, tmp_path, shape):
         if shape == "line":
             assert np.array_equal(u, ref), i
         else:
-            assert _ulps(u, ref) <= 2, (i, _ulps(u, ref))
+            assert np.array_equal(u.reshape(-1, 3)[:, 2], ref.reshape(-1, 3)[:, 2]), i
+            assert _xy_ulps(u, ref) <= 2, (i, _xy_ulps(u, ref))
 
 
 def test_single_object_point_and_default_projector(holo, tmp_path):
@@ -86,23 +92,27 @@ def _curand():
 
 
 def _xorwow_rows(seed, rows, n_random):
-    """The reference's draws for one randomised lattice: per row, n_random uniforms (kept)
-    and n_random * 4 / 32 more (discarded), from one XORWOW generator."""
+    """The reference's numbers for one randomised lattice (cuda/init.h:19-34): one XORWOW
+    device generator; per row, n_random uniforms into the buffer, then n_random * 4 / 32
+    into its start; the row reads the buffer."""
+    import torch
     L = _curand()
     gen = ctypes.c_void_p()
-    assert L.curandCreateGeneratorHost(ctypes.byref(gen), 101) == 0  # CURAND_RNG_PSEUDO_XORWOW
+    assert L.curandCreateGenerator(ctypes.byref(gen), 101) == 0  # CURAND_RNG_PSEUDO_XORWOW
+    buf = torch.zeros(n_random, dtype=torch.float32, device="cuda:0")
+    rows_out = np.zeros((rows, n_random), np.float32)
     try:
         assert L.curandSetPseudoRandomGeneratorSeed(gen, ctypes.c_ulonglong(seed)) == 0
-        keep = np.zeros((rows, n_random), np.float32)
-        junk = np.zeros(max(1, n_random * 4 // 32), np.float32)
         for i in range(rows):
-            assert L.curandGenerateUniform(gen, keep[i].ctypes.data_as(ctypes.c_void_p),
+            assert L.curandGenerateUniform(gen, ctypes.c_void_p(buf.data_ptr()),
                                            ctypes.c_size_t(n_random)) == 0
-            assert L.curandGenerateUniform(gen, junk.ctypes.data_as(ctypes.c_void_p),
+            assert L.curandGenerateUniform(gen, ctypes.c_void_p(buf.data_ptr()),
                                            ctypes.c_size_t(n_random * 4 // 32)) == 0
+            torch.cuda.synchronize()
+            rows_out[i] = buf.cpu().numpy()
     finally:
         L.curandDestroyGenerator(gen)
-    return keep
+    return rows_out
 
 
 def _lattice(n, width, off, aspect, rnd=None):
