@@ -525,6 +525,10 @@ constexpr Variant kVariants[] = {
     {512, 1, 1024, 6, 3, 1, 0, 1, 8},   // 48: as 34
     {512, 1, 1024, 6, 3, 1, 0, 1, 12},  // 49: as 34
     {512, 1, 1024, 7, 3, 1, 0, 1, 4},   // 50: as 36
+    // build flag 16: the next block's first TMEM load during a block's last chunk
+    {512, 1, 1024, 6, 3, 1, 0, 1, 16},  // 51: as 34
+    {512, 1, 1024, 6, 3, 1, 0, 1, 24},  // 52: as 34, with flag 8
+    {512, 1, 1024, 7, 3, 1, 0, 1, 16},  // 53: as 36
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 

@@ -148,8 +148,11 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
 // Build flags: kTcScalar -- the MUFU pairs accumulated in scalar FP32 (no packing);
 // kTcHalfUnroll -- the 16-column chunks of a block in a loop of chunk pairs instead
 // of fully unrolled (half the pair-loop code); kTcRcp -- the target row's 1/Qt and
-// 1/Qt^2 from one correctly rounded reciprocal instead of two divisions.
-constexpr int kTcScalar = 1, kTcHalfUnroll = 4, kTcRcp = 8;
+// 1/Qt^2 from one correctly rounded reciprocal instead of two divisions; kTcPrefetch --
+// during a block's last chunk, if the next block's accumulator is already complete
+// (non-blocking barrier test), its first chunk's TMEM load is issued then instead of
+// after the block (the latency of that load otherwise opens every block).
+constexpr int kTcScalar = 1, kTcHalfUnroll = 4, kTcRcp = 8, kTcPrefetch = 16;
 
 // BATCHED: work items (problem, target tile, source range, split) come from a
 // device queue (atomic counter) and each names its own problem descriptor;
@@ -457,28 +460,47 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
         if (j > sb && tid < kTcTT && !*abort_flag) carry(j - 1);
         // ---- consumers: sin/cos and accumulation of a' e^{i theta'} ----
         const int lg = warp & 3, cg = warp >> 2;
+        uint32_t rv[2][16];
+        bool pre = false;  // kTcPrefetch: chunk 0 of this block already requested into rv[0]
         for (int m = 0; m < 4; ++m) {
           uint64_t re2 = 0ull, im2 = 0ull;
           float res[2] = {0.f, 0.f}, ims[2] = {0.f, 0.f};  // SC: the MUFU pairs
           for (int n = 0; n < NBLK; ++n) {
-            const int b = (m * NBLK + n) & 1;
-            const bool ok =
-                __all_sync(0xffffffffu, tc_wait(&full[b], uses[b] & 1u, abort_flag, err));
-            ++uses[b];
-            ptx::tc_fence_after();
+            const int blk = m * NBLK + n, b = blk & 1;
+            bool ok = true;
+            if (!pre) {
+              ok = __all_sync(0xffffffffu, tc_wait(&full[b], uses[b] & 1u, abort_flag, err));
+              ++uses[b];
+              ptx::tc_fence_after();
+            }
             if (ok) {
               // the load of chunk ch + 1 is in flight while chunk ch is summed
               const uint32_t ta =
                   tbase + ((uint32_t)(32 * lg) << 16) + (uint32_t)(b * kTcN + cg * S::Cols);
-              uint32_t rv[2][16];
-              ptx::tmem_ld16_nowait(ta, rv[0]);
+              if (!pre) ptx::tmem_ld16_nowait(ta, rv[0]);
               ptx::tmem_wait16(rv[0]);
+              pre = false;
+              const int bn = (blk + 1) & 1;  // the next block's accumulator buffer
+              const uint32_t ta_next =
+                  tbase + ((uint32_t)(32 * lg) << 16) + (uint32_t)(bn * kTcN + cg * S::Cols);
               // chunk ch (parity P = ch & 1, a compile-time constant): its phases are in
               // rv[P]; the load of chunk ch + 1 into rv[P ^ 1] is in flight meanwhile
               auto chunk = [&](auto parity, const int ch) {
                 constexpr int P = decltype(parity)::value;
-                if (ch + 1 < S::Chunks)
+                if (ch + 1 < S::Chunks) {
                   ptx::tmem_ld16_nowait(ta + (uint32_t)(16 * (ch + 1)), rv[P ^ 1]);
+                } else if ((FL & kTcPrefetch) && blk + 1 < 4 * NBLK) {
+                  // the last chunk (P = 1, rv[0] free): the next block's first load now,
+                  // if its MMAs are complete already; else after this block as usual
+                  const bool ready = __all_sync(
+                      0xffffffffu, !*abort_flag && ptx::mbar_test_wait(&full[bn], uses[bn] & 1u));
+                  if (ready) {
+                    ++uses[bn];
+                    ptx::tc_fence_after();
+                    ptx::tmem_ld16_nowait(ta_next, rv[P ^ 1]);
+                    pre = true;
+                  }
+                }
                 const float4 *ap =
                     reinterpret_cast<const float4 *>(amp + (j & 1) * kTcCS + n * kTcN +
                                                      cg * S::Cols + 16 * ch);
@@ -630,6 +652,9 @@ int occupancy_tc(int *out) {
   HOLO_TC_CASE(1024, 3, 3, kTcHalfUnroll)     \
   HOLO_TC_CASE(1024, 3, 3, kTcRcp)            \
   HOLO_TC_CASE(1024, 3, 3, kTcHalfUnroll | kTcRcp) \
+  HOLO_TC_CASE(1024, 3, 3, kTcPrefetch)       \
+  HOLO_TC_CASE(1024, 3, 3, kTcPrefetch | kTcRcp) \
+  HOLO_TC_CASE(1024, 3, 4, kTcPrefetch)       \
   HOLO_TC_CASE(1024, 3, 4, 0)                 \
   HOLO_TC_CASE(1024, 3, 4, kTcScalar)         \
   HOLO_TC_CASE(1024, 3, 4, kTcHalfUnroll)     \
