@@ -71,8 +71,7 @@ struct Variant {
   int ws = 0;     // 1: warp-specialised sin/cos (`poly` is then the average per thread)
   int tc = 0;     // 1: phase on the tensor cores (kernel_tc.cu; `poly` of 16 source pairs)
   int sc = 0;     // tc only, build flags: 1 MUFU pairs accumulated in scalar FP32, 4 chunk
-                 // loop half unrolled, 8 one reciprocal for the target row's 1/Qt, 1/Qt^2,
-                 // 16 next block's first TMEM load early, 32 MMA blocks of 128 sources
+                 // loop half unrolled, 8 one reciprocal for the target row's 1/Qt, 1/Qt^2
   int tt() const { return threads * r; }
 };
 
@@ -217,8 +216,7 @@ int launch_gather_apf(const double *amp, const double *phase, const int32_t *ord
 // (1024, 512 or 256: 4 consumer warps per TMEM lane group and MMA blocks of 256
 // sources; 768: 6 consumer warps, blocks of 192), `poly16` of every 16 source pairs
 // on the FMA-pipe sin/cos, `flags` (Variant.sc): 1 MUFU pairs accumulated unpacked, 4
-// chunk loop half unrolled, 8 one reciprocal for the target row's 1/Qt and 1/Qt^2, 16
-// the next block's first TMEM load early, 32 MMA blocks of 128 sources (four buffers)
+// chunk loop half unrolled, 8 one reciprocal for the target row's 1/Qt and 1/Qt^2
 int launch_split_tc(const SplitProblem &p, int cs, int poly16, int flags, int grid, int *err,
                     cudaStream_t s);
 int split_tc_occupancy(int cs, int poly16, int flags, int *ctas_per_sm);

@@ -529,11 +529,6 @@ constexpr Variant kVariants[] = {
     {512, 1, 1024, 6, 3, 1, 0, 1, 16},  // 51: as 34
     {512, 1, 1024, 6, 3, 1, 0, 1, 24},  // 52: as 34, with flag 8
     {512, 1, 1024, 7, 3, 1, 0, 1, 16},  // 53: as 36
-    // build flag 32: MMA blocks of 128 sources in four tensor-memory buffers
-    {512, 1, 1024, 6, 3, 1, 0, 1, 32},  // 54: as 34
-    {512, 1, 1024, 6, 3, 1, 0, 1, 56},  // 55: as 34, with flags 8 and 16
-    {512, 1, 1024, 7, 3, 1, 0, 1, 56},  // 56: as 36, with flags 8 and 16
-    {512, 1, 512, 6, 3, 1, 0, 1, 56},   // 57: as 44, with flags 8 and 16
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 

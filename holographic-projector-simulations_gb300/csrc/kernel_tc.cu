@@ -53,30 +53,14 @@ constexpr int kTcM = 128, kTcK = 8;
 constexpr int kTcCols = 512;                  // TMEM columns allocated: two accumulator buffers
 constexpr uint32_t kTcLbo = 128, kTcSbo = 256;  // operand layout (bytes), see tc_off
 
-// Build flags: kTcScalar -- the MUFU pairs accumulated in scalar FP32 (no packing);
-// kTcHalfUnroll -- the 16-column chunks of a block in a loop of chunk pairs instead
-// of fully unrolled (half the pair-loop code); kTcRcp -- the target row's 1/Qt and
-// 1/Qt^2 from one correctly rounded reciprocal instead of two divisions; kTcPrefetch --
-// during a block's last chunk, if the next block's accumulator is already complete
-// (non-blocking barrier test), its first chunk's TMEM load is issued then instead of
-// after the block (the latency of that load otherwise opens every block); kTcNarrow --
-// MMA blocks of 128 sources in four tensor-memory buffers instead of 256 in two: the
-// MMAs then run up to three blocks ahead of the slowest consumer warp instead of one,
-// so a warp that is ahead waits less for the next block (each warp reads 32 columns,
-// two chunks, per block).
-constexpr int kTcScalar = 1, kTcHalfUnroll = 4, kTcRcp = 8, kTcPrefetch = 16, kTcNarrow = 32;
-
 // Shape of one build: CG column groups of consumer warps per TMEM lane group (4 lane
-// groups of 32 targets), NB sources per MMA block (TMEM columns per buffer), NBUF
-// accumulator buffers, CS = NBLK NB sources per tile.  CG = 4: 16 consumer warps, NB 256
-// (128 with kTcNarrow); CG = 6: 24 warps, NB 192.
-template <int CG, int NBLK, int FL>
+// groups of 32 targets), NB sources per MMA block (TMEM columns per buffer), CS = NBLK NB
+// sources per tile.  CG = 4: 16 consumer warps, NB 256; CG = 6: 24 warps, NB 192.
+template <int CG, int NBLK>
 struct TcShape {
   static_assert(CG == 4 || CG == 6, "tensor-core split kernel: 4 or 6 column groups");
-  static_assert(!(FL & kTcNarrow) || CG == 4, "tensor-core split kernel: narrow blocks need CG 4");
-  static constexpr int NB = (FL & kTcNarrow) ? 128 : CG == 4 ? 256 : 192;
-  static constexpr int NBUF = kTcCols / NB;       // accumulator buffers in tensor memory
-  static_assert(NBLK >= 1 && NBLK * NB <= 1024, "tensor-core split kernel: at most 1024 sources");
+  static_assert(NBLK == 1 || NBLK == 2 || NBLK == 4, "tensor-core split kernel: 1, 2 or 4 blocks");
+  static constexpr int NB = CG == 4 ? 256 : 192;
   static constexpr int CS = NBLK * NB;
   static constexpr int Consumers = 4 * CG;        // consumer warps
   static constexpr int Threads = 32 * (Consumers + 2);  // + the MMA warp + the frame warp
@@ -92,10 +76,9 @@ __host__ __device__ __forceinline__ int tc_off(int r, int k) {
   return (r >> 3) * 64 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3);
 }
 
-template <int CG, int NBLK, int FL>
+template <int CG, int NBLK>
 struct TcSmem {
-  static constexpr int kTcCS = TcShape<CG, NBLK, FL>::CS;
-  static constexpr int NBUF = TcShape<CG, NBLK, FL>::NBUF;
+  static constexpr int kTcCS = TcShape<CG, NBLK>::CS;
   static constexpr size_t raw_geo = 0;                                 // float [CS*6]
   static constexpr size_t raw_apf = raw_geo + kTcCS * 6 * 4;           // float2 [CS]
   static constexpr size_t opb_hi = raw_apf + kTcCS * 8;                // float [CS*8]
@@ -105,31 +88,29 @@ struct TcSmem {
   static constexpr size_t opa_lo = opa_hi + kTcTT * kTcK * 4;          // float [TT*8]
   static constexpr size_t opa_one = opa_lo + kTcTT * kTcK * 4;         // float [128*8]: (1,1,1,0..)
   static constexpr size_t amp = opa_one + kTcM * kTcK * 4;             // float [2][CS]
-  // partial sums, [PB][CG][TT] float2: a tile's are carried during the next tile.  A
-  // consumer rewrites them after the tile's block NBLK - 1, whose MMA waits for every
-  // consumer to free block NBLK - 1 - NBUF: with NBLK > NBUF that block is of the same
-  // tile, so every consumer has carried them; otherwise two buffers
-  static constexpr int PB = NBLK > NBUF ? 1 : 2;
+  // partial sums, [PB][CG][TT] float2: a tile's are carried during the next tile, and
+  // with fewer than three source blocks per tile a consumer can write the next
+  // tile's before a slower one has carried them, so those builds keep two buffers
+  static constexpr int PB = NBLK >= 3 ? 1 : 2;
   static constexpr size_t part = amp + 2 * kTcCS * 4;
   static constexpr size_t acc = part + PB * CG * kTcTT * 8;            // float4 [TT]
   static constexpr size_t tph = acc + kTcTT * 16;                      // float [2][TT]
   static constexpr size_t tsc = tph + 2 * kTcTT * 4;                   // float [2][TT]
   static constexpr size_t tgeo = tsc + 2 * kTcTT * 4;                  // float [6][TT]
   static constexpr size_t frame = tgeo + 6 * kTcTT * 4;                // Frame [2]
-  // uint64: bulk copy, full[NBUF], free[NBUF], frame ready
-  static constexpr size_t bars = (frame + 2 * sizeof(Frame) + 15) / 16 * 16;
-  static constexpr size_t misc = bars + (2 + 2 * NBUF) * 8;            // uint32 taddr, abort
+  static constexpr size_t bars = (frame + 2 * sizeof(Frame) + 15) / 16 * 16;  // uint64 [6]
+  static constexpr size_t misc = bars + 6 * 8;                         // uint32 taddr, abort
   static constexpr size_t bytes = misc + 16;
 };
-template <int CG, int NBLK, int FL>
+template <int CG, int NBLK>
 constexpr bool tc_layout_ok() {
-  using L = TcSmem<CG, NBLK, FL>;
+  using L = TcSmem<CG, NBLK>;
   return L::bytes <= 227 * 1024 && L::raw_apf % 16 == 0 && L::opb_hi % 128 == 0 &&
          L::opb_lo % 128 == 0 && L::opb_a % 128 == 0 && L::opa_hi % 128 == 0 &&
          L::opa_lo % 128 == 0 && L::opa_one % 128 == 0 && L::amp % 16 == 0 && L::acc % 16 == 0;
 }
-static_assert(tc_layout_ok<4, 4, 0>() && tc_layout_ok<4, 2, 0>() && tc_layout_ok<4, 1, 0>() &&
-                  tc_layout_ok<6, 4, 0>() && tc_layout_ok<4, 8, kTcNarrow>(),
+static_assert(tc_layout_ok<4, 4>() && tc_layout_ok<4, 2>() && tc_layout_ok<4, 1>() &&
+                  tc_layout_ok<6, 4>(),
               "tensor-core split kernel: shared memory size and operand alignment");
 
 __device__ __forceinline__ void split_range_tc(int n, int splits, int s, int *b, int *e) {
@@ -164,18 +145,25 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
   return false;
 }
 
+// Build flags: kTcScalar -- the MUFU pairs accumulated in scalar FP32 (no packing);
+// kTcHalfUnroll -- the 16-column chunks of a block in a loop of chunk pairs instead
+// of fully unrolled (half the pair-loop code); kTcRcp -- the target row's 1/Qt and
+// 1/Qt^2 from one correctly rounded reciprocal instead of two divisions; kTcPrefetch --
+// during a block's last chunk, if the next block's accumulator is already complete
+// (non-blocking barrier test), its first chunk's TMEM load is issued then instead of
+// after the block (the latency of that load otherwise opens every block).
+constexpr int kTcScalar = 1, kTcHalfUnroll = 4, kTcRcp = 8, kTcPrefetch = 16;
 
 // BATCHED: work items (problem, target tile, source range, split) come from a
 // device queue (atomic counter) and each names its own problem descriptor;
 // otherwise item i of problem P0 is target tile i / splits, split i % splits.
 template <int CG, int NBLK, int NPP0, int NPP1, int FL, bool BATCHED>
-__global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
+__global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
     k_split_tc(const SplitProblem P0, const SplitProblem *__restrict__ probs,
                const WorkItem *__restrict__ items, int n_items, int *queue, int *err) {
   extern __shared__ __align__(128) unsigned char smem[];
-  using L = TcSmem<CG, NBLK, FL>;
-  using S = TcShape<CG, NBLK, FL>;
-  constexpr int NBUF = S::NBUF;
+  using L = TcSmem<CG, NBLK>;
+  using S = TcShape<CG, NBLK>;
   constexpr int kTcCS = S::CS, kTcN = S::NB, kTcConsumers = S::Consumers;
   constexpr int kTcThreads = S::Threads;
   float *raw_geo = reinterpret_cast<float *>(smem + L::raw_geo);
@@ -196,8 +184,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
   float *tgeo = reinterpret_cast<float *>(smem + L::tgeo);  // this item's target records
   Frame *frames = reinterpret_cast<Frame *>(smem + L::frame);  // tile j in frames[j & 1]
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bars);
-  uint64_t *bar_tma = bars, *full = bars + 1, *freeb = bars + 1 + NBUF,
-           *frame_ready = bars + 1 + 2 * NBUF;
+  uint64_t *bar_tma = bars, *full = bars + 1, *freeb = bars + 3, *frame_ready = bars + 5;
   uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(smem + L::misc);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + L::misc + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -208,10 +195,10 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
 
   if (tid == 0) {
     ptx::mbar_init(bar_tma, 1);
-    for (int b = 0; b < NBUF; ++b) {
-      ptx::mbar_init(&full[b], 1);
-      ptx::mbar_init(&freeb[b], kTcConsumers);
-    }
+    ptx::mbar_init(&full[0], 1);
+    ptx::mbar_init(&full[1], 1);
+    ptx::mbar_init(&freeb[0], kTcConsumers);
+    ptx::mbar_init(&freeb[1], kTcConsumers);
     ptx::mbar_init(frame_ready, 1);
     *abort_flag = 0;
     ptx::fence_barrier_init();
@@ -228,11 +215,8 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
 
   constexpr uint32_t idesc = ptx::tc_idesc_tf32(kTcM, kTcN);
   uint32_t par_tma = 0, n_frames = 0;
-  // running block number (producer: MMA groups issued; consumers: blocks consumed) over
-  // all tiles of this CTA: block g lives in buffer g % NBUF, and it is that buffer's use
-  // g / NBUF, whose barrier phases have parity (g / NBUF) & 1.  Every tile has 4 NBLK
-  // blocks, a multiple of NBUF, so g % NBUF is also the block's index in its tile % NBUF.
-  uint32_t gq = 0u;
+  // producer: MMA groups issued per TMEM buffer; consumers: completions consumed
+  uint32_t uses[2] = {0u, 0u};
   __shared__ int s_item;
 
   for (int it = 0;; ++it) {
@@ -447,8 +431,8 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
         // ---- MMA issue: 4 target blocks x NBLK source blocks, double-buffered ----
         if (lane == 0) {
           for (int blk = 0; blk < 4 * NBLK; ++blk) {
-            const int m = blk / NBLK, n = blk % NBLK, b = blk % NBUF;
-            if (gq >= (uint32_t)NBUF) tc_wait(&freeb[b], (gq / NBUF - 1) & 1u, abort_flag, err);
+            const int m = blk / NBLK, n = blk % NBLK, b = blk & 1;
+            if (uses[b] > 0) tc_wait(&freeb[b], (uses[b] - 1) & 1u, abort_flag, err);
             if (*abort_flag) break;
             ptx::tc_fence_after();
             const uint32_t d = tbase + (uint32_t)(b * kTcN);
@@ -463,7 +447,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
             ptx::tc_mma_tf32(d, dal, dbh, idesc, 1u);
             ptx::tc_mma_tf32(d, d1, dba, idesc, 1u);
             ptx::tc_commit(&full[b]);
-            ++gq;
+            ++uses[b];
           }
         }
         __syncwarp();
@@ -482,11 +466,11 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
           uint64_t re2 = 0ull, im2 = 0ull;
           float res[2] = {0.f, 0.f}, ims[2] = {0.f, 0.f};  // SC: the MUFU pairs
           for (int n = 0; n < NBLK; ++n) {
-            const int blk = m * NBLK + n, b = blk % NBUF;
+            const int blk = m * NBLK + n, b = blk & 1;
             bool ok = true;
             if (!pre) {
-              ok = __all_sync(0xffffffffu, tc_wait(&full[b], (gq / NBUF) & 1u, abort_flag, err));
-              ++gq;
+              ok = __all_sync(0xffffffffu, tc_wait(&full[b], uses[b] & 1u, abort_flag, err));
+              ++uses[b];
               ptx::tc_fence_after();
             }
             if (ok) {
@@ -496,7 +480,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
               if (!pre) ptx::tmem_ld16_nowait(ta, rv[0]);
               ptx::tmem_wait16(rv[0]);
               pre = false;
-              const int bn = (blk + 1) % NBUF;  // the next block's accumulator buffer
+              const int bn = (blk + 1) & 1;  // the next block's accumulator buffer
               const uint32_t ta_next =
                   tbase + ((uint32_t)(32 * lg) << 16) + (uint32_t)(bn * kTcN + cg * S::Cols);
               // chunk ch (parity P = ch & 1, a compile-time constant): its phases are in
@@ -509,10 +493,9 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
                   // the last chunk (P = 1, rv[0] free): the next block's first load now,
                   // if its MMAs are complete already; else after this block as usual
                   const bool ready = __all_sync(
-                      0xffffffffu,
-                      !*abort_flag && ptx::mbar_test_wait(&full[bn], (gq / NBUF) & 1u));
+                      0xffffffffu, !*abort_flag && ptx::mbar_test_wait(&full[bn], uses[bn] & 1u));
                   if (ready) {
-                    ++gq;
+                    ++uses[bn];
                     ptx::tc_fence_after();
                     ptx::tmem_ld16_nowait(ta_next, rv[P ^ 1]);
                     pre = true;
@@ -610,9 +593,8 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
 
   // ---- teardown: the MMAs this CTA issued have completed, then free the TMEM ----
   if (producer && lane == 0)
-    for (int b = 0; b < NBUF; ++b)
-      if (gq > (uint32_t)b)  // the last of the (gq - 1 - b) / NBUF + 1 commits into buffer b
-        ptx::mbar_wait_bounded(&full[b], ((gq - 1 - b) / NBUF) & 1u, kWaitCycles);
+    for (int b = 0; b < 2; ++b)
+      if (uses[b] > 0) ptx::mbar_wait_bounded(&full[b], (uses[b] - 1) & 1u, kWaitCycles);
   ptx::tc_fence_before();
   __syncthreads();
   ptx::tc_fence_after();
@@ -622,8 +604,8 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK, FL>::Threads, 1)
 template <int CG, int NBLK, int NPP0, int NPP1, int FL>
 int launch_tc(const SplitProblem &p, int grid, int *err, cudaStream_t s) {
   auto kern = k_split_tc<CG, NBLK, NPP0, NPP1, FL, false>;
-  constexpr int bytes = (int)TcSmem<CG, NBLK, FL>::bytes;
-  constexpr int threads = TcShape<CG, NBLK, FL>::Threads;
+  constexpr int bytes = (int)TcSmem<CG, NBLK>::bytes;
+  constexpr int threads = TcShape<CG, NBLK>::Threads;
   HOLO_TRY((kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, FL, false>>(threads, bytes, nullptr)));
   const int n_items = p.n_ttiles * p.splits;
   if (n_items <= 0) return HOLO_OK;
@@ -637,8 +619,8 @@ template <int CG, int NBLK, int NPP0, int NPP1, int FL>
 int launch_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_items, int *queue,
                       int grid, int *err, cudaStream_t s) {
   auto kern = k_split_tc<CG, NBLK, NPP0, NPP1, FL, true>;
-  constexpr int bytes = (int)TcSmem<CG, NBLK, FL>::bytes;
-  constexpr int threads = TcShape<CG, NBLK, FL>::Threads;
+  constexpr int bytes = (int)TcSmem<CG, NBLK>::bytes;
+  constexpr int threads = TcShape<CG, NBLK>::Threads;
   HOLO_TRY((kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, FL, true>>(threads, bytes, nullptr)));
   kern<<<grid, threads, bytes, s>>>(SplitProblem{}, probs, items, n_items, queue, err);
   note_launches(1);
@@ -648,8 +630,8 @@ int launch_tc_batched(const SplitProblem *probs, const WorkItem *items, int n_it
 
 template <int CG, int NBLK, int NPP0, int NPP1, int FL>
 int occupancy_tc(int *out) {
-  constexpr int bytes = (int)TcSmem<CG, NBLK, FL>::bytes;
-  return kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, FL, false>>(TcShape<CG, NBLK, FL>::Threads,
+  constexpr int bytes = (int)TcSmem<CG, NBLK>::bytes;
+  return kernel_setup<k_split_tc<CG, NBLK, NPP0, NPP1, FL, false>>(TcShape<CG, NBLK>::Threads,
                                                                    bytes, out);
 }
 
@@ -659,10 +641,9 @@ int occupancy_tc(int *out) {
 // 6 column groups, the others CS / 256 blocks of 256 with 4.  A use site defines
 // CALL(CG, NBLK, A, B, FL) and expands HOLO_TC_SWITCH.
 #define HOLO_TC_KEY(CS, NP16, FLAGS) ((CS) * 1000 + (NP16) * 10 + (FLAGS))
-#define HOLO_TC_CASE(CS, A, B, FL)                                          \
-  case HOLO_TC_KEY(CS, (A) + (B), FL):                                      \
-    return CALL(((CS) == 768 ? 6 : 4),                                      \
-                ((CS) == 768 ? 4 : ((FL) & kTcNarrow) ? (CS) / 128 : (CS) / 256), A, B, FL);
+#define HOLO_TC_CASE(CS, A, B, FL)     \
+  case HOLO_TC_KEY(CS, (A) + (B), FL): \
+    return CALL(((CS) == 768 ? 6 : 4), ((CS) == 768 ? 4 : (CS) / 256), A, B, FL);
 #define HOLO_TC_BUILDS                        \
   HOLO_TC_CASE(1024, 2, 2, 0)                 \
   HOLO_TC_CASE(1024, 2, 3, 0)                 \
@@ -674,10 +655,6 @@ int occupancy_tc(int *out) {
   HOLO_TC_CASE(1024, 3, 3, kTcPrefetch)       \
   HOLO_TC_CASE(1024, 3, 3, kTcPrefetch | kTcRcp) \
   HOLO_TC_CASE(1024, 3, 4, kTcPrefetch)       \
-  HOLO_TC_CASE(1024, 3, 3, kTcNarrow)         \
-  HOLO_TC_CASE(1024, 3, 3, kTcNarrow | kTcPrefetch | kTcRcp) \
-  HOLO_TC_CASE(1024, 3, 4, kTcNarrow | kTcPrefetch | kTcRcp) \
-  HOLO_TC_CASE(512, 3, 3, kTcNarrow | kTcPrefetch | kTcRcp) \
   HOLO_TC_CASE(1024, 3, 4, 0)                 \
   HOLO_TC_CASE(1024, 3, 4, kTcScalar)         \
   HOLO_TC_CASE(1024, 3, 4, kTcHalfUnroll)     \
