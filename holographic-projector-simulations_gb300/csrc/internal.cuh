@@ -71,7 +71,9 @@ struct Variant {
   int ws = 0;     // 1: warp-specialised sin/cos (`poly` is then the average per thread)
   int tc = 0;     // 1: phase on the tensor cores (kernel_tc.cu; `poly` of 16 source pairs)
   int sc = 0;     // tc only, build flags: 1 MUFU pairs accumulated in scalar FP32, 4 chunk
-                 // loop half unrolled, 8 one reciprocal for the target row's 1/Qt, 1/Qt^2
+                 // loop half unrolled, 8 one reciprocal for the target row's 1/Qt, 1/Qt^2,
+                 // 16 next block's first TMEM load early, 32 / 64 the MMA warp's /
+                 // consumers' waits sleep between polls
   int tt() const { return threads * r; }
 };
 

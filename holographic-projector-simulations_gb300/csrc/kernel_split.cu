@@ -529,6 +529,19 @@ constexpr Variant kVariants[] = {
     {512, 1, 1024, 6, 3, 1, 0, 1, 16},  // 51: as 34
     {512, 1, 1024, 6, 3, 1, 0, 1, 24},  // 52: as 34, with flag 8
     {512, 1, 1024, 7, 3, 1, 0, 1, 16},  // 53: as 36
+    // build flags 32 / 64: the MMA warp's / the consumers' waits sleep between polls
+    {512, 1, 1024, 6, 3, 1, 0, 1, 32},  // 54: as 34
+    {512, 1, 1024, 6, 3, 1, 0, 1, 96},  // 55: as 34
+    {512, 1, 1024, 6, 3, 1, 0, 1, 48},  // 56: as 51
+    // build flags 128 (polynomial columns in half turns from the tensor cores) and 256
+    // (degree-7 sine): cheaper FMA-pipe sin/cos, so more polynomial pairs
+    {512, 1, 1024, 6, 3, 1, 0, 1, 128},   // 57: as 34
+    {512, 1, 1024, 6, 3, 1, 0, 1, 384},   // 58: as 34
+    {512, 1, 1024, 7, 3, 1, 0, 1, 384},   // 59: 7 of 16
+    {512, 1, 1024, 8, 3, 1, 0, 1, 384},   // 60: 8 of 16
+    {512, 1, 1024, 9, 3, 1, 0, 1, 384},   // 61: 9 of 16
+    {512, 1, 1024, 7, 3, 1, 0, 1, 432},   // 62: as 59, with flags 16 and 32
+    {512, 1, 1024, 8, 3, 1, 0, 1, 432},   // 63: as 60, with flags 16 and 32
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 

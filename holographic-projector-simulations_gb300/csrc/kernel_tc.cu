@@ -135,11 +135,14 @@ __device__ __forceinline__ void store_row_split(float *hi, float *lo, int r, con
   *reinterpret_cast<float4 *>(lo + tc_off(r, 4)) = make_float4(l[4], l[5], l[6], l[7]);
 }
 
-// Bounded wait that gives up at once when the CTA has aborted.
+// Bounded wait that gives up at once when the CTA has aborted; sleep_ns > 0: poll with
+// that much sleep in between.
 __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
-                                        int *err) {
+                                        int *err, unsigned sleep_ns = 0) {
   if (*abort_flag) return false;
-  if (ptx::mbar_wait_bounded(bar, parity, kWaitCycles)) return true;
+  if (sleep_ns ? ptx::mbar_wait_bounded_sleep(bar, parity, kWaitCycles, sleep_ns)
+               : ptx::mbar_wait_bounded(bar, parity, kWaitCycles))
+    return true;
   *abort_flag = 1;
   atomicExch(err, kDevErrTimeout);
   return false;
@@ -151,8 +154,17 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
 // 1/Qt^2 from one correctly rounded reciprocal instead of two divisions; kTcPrefetch --
 // during a block's last chunk, if the next block's accumulator is already complete
 // (non-blocking barrier test), its first chunk's TMEM load is issued then instead of
-// after the block (the latency of that load otherwise opens every block).
-constexpr int kTcScalar = 1, kTcHalfUnroll = 4, kTcRcp = 8, kTcPrefetch = 16;
+// after the block (the latency of that load otherwise opens every block);
+// kTcSleepMma / kTcSleepUse -- the MMA warp's waits for free buffers / the consumers'
+// waits for complete blocks poll with a short sleep in between (a spinning warp takes
+// issue slots from the four consumer warps of its SM sub-partition); kTcHalfTurns --
+// the source rows of the polynomial columns are scaled by 1 / pi in the operand build,
+// so the tensor cores deliver their phases in half turns and the polynomial needs no
+// multiply; kTcSin7 -- with kTcHalfTurns, a sine of degree 7 instead of 9.  Together
+// they take the FMA-pipe sin/cos from 16 to 14 lane operations per source, so more
+// source pairs can leave the XU pipe.
+constexpr int kTcScalar = 1, kTcHalfUnroll = 4, kTcRcp = 8, kTcPrefetch = 16, kTcSleepMma = 32,
+              kTcSleepUse = 64, kTcHalfTurns = 128, kTcSin7 = 256;
 
 // BATCHED: work items (problem, target tile, source range, split) come from a
 // device queue (atomic counter) and each names its own problem descriptor;
@@ -387,9 +399,21 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
             const float s2 = fmaf(Sx, Sx, Sy * Sy);
             g[r][0] = s2; g[r][1] = Sx; g[r][2] = Sy; g[r][3] = Ps;
             g[r][4] = Ps * s2; g[r][5] = Ps * Sx; g[r][6] = Ps * Sy;
+            float sAh = sA;
+            if (FL & kTcHalfTurns) {
+              // column of row i in its block, and whether the pair loop takes its sin/cos
+              // from the polynomial (source pair pp < npp of its 16-column chunk)
+              const int c = (i % kTcN) % S::Cols, pp = (c % 16) / 2;
+              if (pp < (((c / 16) & 1) ? NPP1 : NPP0)) {
+                constexpr float kInvPi = 0.318309886f;
+#pragma unroll
+                for (int k = 0; k < kTcK; ++k) g[r][k] *= kInvPi;
+                sAh = sA * kInvPi;
+              }
+            }
             // sign A = a0 + a1 + a2 exactly, each part a TF32 number
-            a3[r][0] = ptx::to_tf32_int(sA);
-            const float r1 = __fsub_rn(sA, a3[r][0]);
+            a3[r][0] = ptx::to_tf32_int(sAh);
+            const float r1 = __fsub_rn(sAh, a3[r][0]);
             a3[r][1] = ptx::to_tf32_int(r1);
             a3[r][2] = ptx::to_tf32_int(__fsub_rn(r1, a3[r][1]));
             am[r] = pa.y * fmaf(Ps, ir0, 1.f);
@@ -432,7 +456,9 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
         if (lane == 0) {
           for (int blk = 0; blk < 4 * NBLK; ++blk) {
             const int m = blk / NBLK, n = blk % NBLK, b = blk & 1;
-            if (uses[b] > 0) tc_wait(&freeb[b], (uses[b] - 1) & 1u, abort_flag, err);
+            if (uses[b] > 0)
+              tc_wait(&freeb[b], (uses[b] - 1) & 1u, abort_flag, err,
+                      (FL & kTcSleepMma) ? 64u : 0u);
             if (*abort_flag) break;
             ptx::tc_fence_after();
             const uint32_t d = tbase + (uint32_t)(b * kTcN);
@@ -469,7 +495,8 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
             const int blk = m * NBLK + n, b = blk & 1;
             bool ok = true;
             if (!pre) {
-              ok = __all_sync(0xffffffffu, tc_wait(&full[b], uses[b] & 1u, abort_flag, err));
+              ok = __all_sync(0xffffffffu, tc_wait(&full[b], uses[b] & 1u, abort_flag, err,
+                                                   (FL & kTcSleepUse) ? 32u : 0u));
               ++uses[b];
               ptx::tc_fence_after();
             }
@@ -532,7 +559,10 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
                   uint64_t sn, cs;
                   if (pp < npp) {
                     uint64_t sign;
-                    poly_sincos2_half(t2, sn, cs, sign);  // FMA pipe
+                    if (FL & kTcHalfTurns)
+                      poly_sincos2_ht<(FL & kTcSin7) != 0>(t2, sn, cs, sign);  // FMA pipe
+                    else
+                      poly_sincos2_half(t2, sn, cs, sign);  // FMA pipe
                     am ^= sign;
                   } else {
                     sn = ptx::pack2(ptx::sin_approx(t0), ptx::sin_approx(t1));  // XU pipe
@@ -640,7 +670,7 @@ int occupancy_tc(int *out) {
 // arguments come from the same four numbers: 768-source tiles are 4 blocks of 192 with
 // 6 column groups, the others CS / 256 blocks of 256 with 4.  A use site defines
 // CALL(CG, NBLK, A, B, FL) and expands HOLO_TC_SWITCH.
-#define HOLO_TC_KEY(CS, NP16, FLAGS) ((CS) * 1000 + (NP16) * 10 + (FLAGS))
+#define HOLO_TC_KEY(CS, NP16, FLAGS) ((CS) * 100000 + (NP16) * 1000 + (FLAGS))
 #define HOLO_TC_CASE(CS, A, B, FL)     \
   case HOLO_TC_KEY(CS, (A) + (B), FL): \
     return CALL(((CS) == 768 ? 6 : 4), ((CS) == 768 ? 4 : (CS) / 256), A, B, FL);
@@ -655,6 +685,16 @@ int occupancy_tc(int *out) {
   HOLO_TC_CASE(1024, 3, 3, kTcPrefetch)       \
   HOLO_TC_CASE(1024, 3, 3, kTcPrefetch | kTcRcp) \
   HOLO_TC_CASE(1024, 3, 4, kTcPrefetch)       \
+  HOLO_TC_CASE(1024, 3, 3, kTcSleepMma)       \
+  HOLO_TC_CASE(1024, 3, 3, kTcSleepMma | kTcSleepUse) \
+  HOLO_TC_CASE(1024, 3, 3, kTcSleepMma | kTcPrefetch) \
+  HOLO_TC_CASE(1024, 3, 3, kTcHalfTurns)      \
+  HOLO_TC_CASE(1024, 3, 3, kTcHalfTurns | kTcSin7) \
+  HOLO_TC_CASE(1024, 3, 4, kTcHalfTurns | kTcSin7) \
+  HOLO_TC_CASE(1024, 4, 4, kTcHalfTurns | kTcSin7) \
+  HOLO_TC_CASE(1024, 4, 5, kTcHalfTurns | kTcSin7) \
+  HOLO_TC_CASE(1024, 3, 4, kTcHalfTurns | kTcSin7 | kTcPrefetch | kTcSleepMma) \
+  HOLO_TC_CASE(1024, 4, 4, kTcHalfTurns | kTcSin7 | kTcPrefetch | kTcSleepMma) \
   HOLO_TC_CASE(1024, 3, 4, 0)                 \
   HOLO_TC_CASE(1024, 3, 4, kTcScalar)         \
   HOLO_TC_CASE(1024, 3, 4, kTcHalfUnroll)     \

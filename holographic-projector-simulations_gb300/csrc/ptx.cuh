@@ -66,6 +66,19 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
   return true;
 }
 
+// The same bounded wait, sleeping `ns` nanoseconds between polls: a waiting warp then
+// leaves the issue slots of its SM sub-partition to the warps that have work.
+__device__ __forceinline__ bool mbar_wait_bounded_sleep(uint64_t *bar, uint32_t parity,
+                                                        long long max_cycles, unsigned ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > max_cycles) return false;
+    __nanosleep(ns);
+  }
+  return true;
+}
+
 // 1-D bulk copy global -> shared, completion counted on `bar` (bytes % 16 == 0,
 // both addresses 16-byte aligned).
 __device__ __forceinline__ void bulk_g2s(void *dst_smem, const void *src_gmem, uint32_t bytes,

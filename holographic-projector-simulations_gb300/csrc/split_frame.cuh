@@ -154,6 +154,38 @@ __device__ __forceinline__ void poly_sincos2_half(uint64_t th, uint64_t &sn, uin
   sign = (u << 31) & 0x8000000080000000ull;  // bit 0 of each half: n odd
 }
 
+// The same as poly_sincos2_half for angles given in half turns already, h = theta / pi
+// (the tensor-core kernel scales the phase of its polynomial columns by 1 / pi in the
+// operand build, so the first multiply goes), with a sine of degree 7 when SIN7 (float32
+// Horner error 7.4e-7 on |g| <= 1/2, the size of MUFU sin.approx's own error; fitted by
+// gen_sincos_poly.py) instead of 9.  SIN7 saves one more packed FMA: 12 packed FP32
+// instructions per two angles against 14.
+template <bool SIN7>
+__device__ __forceinline__ void poly_sincos2_ht(uint64_t h, uint64_t &sn, uint64_t &cs,
+                                                uint64_t &sign) {
+  const uint64_t u = ptx::add2(h, splat2(12582912.0f));  // rint(h) in the low bits
+  const uint64_t g = ptx::sub2(h, ptx::sub2(u, splat2(12582912.0f)));
+  const uint64_t g2 = ptx::mul2(g, g);
+  uint64_t s;
+  if (SIN7) {
+    s = ptx::fma2(splat2(-5.546361804e-01f), g2, splat2(2.541898966e+00f));
+    s = ptx::fma2(s, g2, splat2(-5.167142868e+00f));
+    s = ptx::fma2(s, g2, splat2(3.141582012e+00f));
+  } else {
+    s = ptx::fma2(splat2(7.722012699e-02f), g2, splat2(-5.980451703e-01f));
+    s = ptx::fma2(s, g2, splat2(2.550031424e+00f));
+    s = ptx::fma2(s, g2, splat2(-5.167706966e+00f));
+    s = ptx::fma2(s, g2, splat2(3.141592503e+00f));
+  }
+  uint64_t c = ptx::fma2(splat2(2.196968049e-01f), g2, splat2(-1.331880212e+00f));
+  c = ptx::fma2(c, g2, splat2(4.058412075e+00f));
+  c = ptx::fma2(c, g2, splat2(-4.934792995e+00f));
+  c = ptx::fma2(c, g2, splat2(9.999999404e-01f));
+  sn = ptx::mul2(s, g);
+  cs = c;
+  sign = (u << 31) & 0x8000000080000000ull;  // bit 0 of each half: n odd
+}
+
 // poly_sincos on a packed pair of angles (fma.rn.f32x2 and friends): the same
 // polynomial and operation order as poly_sincos, two angles per instruction.
 __device__ __forceinline__ void poly_sincos2(uint64_t th, uint64_t &sn, uint64_t &cs) {

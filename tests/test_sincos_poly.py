@@ -11,6 +11,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 CSRC = os.path.join(os.path.dirname(__file__), "..", "holographic-projector-simulations_gb300",
                     "csrc")
@@ -116,3 +117,33 @@ def test_half_turn_sign_at_quadrant_boundaries():
         x = th.astype(np.float64)
         assert np.abs(s - np.sin(x)).max() < 1.5e-6
         assert np.abs(c - np.cos(x)).max() < 1.5e-6
+
+
+def half_turns_given(h, sin7):
+    """poly_sincos2_ht: the angle arrives in half turns (h = theta / pi); SIN7 selects the
+    degree-7 sine (the first of the two sine coefficient sets in the source)."""
+    body = _body("poly_sincos2_ht")
+    k = _floats(body)
+    assert len(k) == 4 + 5 + 5  # degree-7 sine, degree-9 sine, degree-8 cosine
+    s_c = k[0:4] if sin7 else k[4:9]
+    c_c = k[9:14]
+    u = _rnd(h.astype(np.float64) + MAGIC)
+    g = _rnd(h.astype(np.float64) - _rnd(u.astype(np.float64) - MAGIC))
+    g2 = _rnd(g.astype(np.float64) * g)
+    s = _rnd(_horner(s_c, g2).astype(np.float64) * g)
+    c = _horner(c_c, g2)
+    sign = np.where((u.view(np.uint32) & 1) == 1, -1.0, 1.0)
+    return sign * s, sign * c
+
+
+@pytest.mark.parametrize("sin7,bound", [(True, 8.0e-7), (False, 2.5e-7)])
+def test_half_turns_given_within_bound(sin7, bound):
+    # the tensor cores deliver h = theta / pi; over two turns of theta
+    h = np.linspace(-2.0, 2.0, 400_001).astype(F32)
+    s, c = half_turns_given(h, sin7)
+    x = np.pi * h.astype(np.float64)
+    assert np.abs(s - np.sin(x)).max() <= bound
+    assert np.abs(c - np.cos(x)).max() <= 3.5e-7
+    # the degree-9 set is the one poly_sincos2_half uses
+    if not sin7:
+        assert _floats(_body("poly_sincos2_ht"))[4:] == _floats(_body("poly_sincos2_half"))[1:]
