@@ -542,6 +542,13 @@ constexpr Variant kVariants[] = {
     {512, 1, 1024, 9, 3, 1, 0, 1, 384},   // 61: 9 of 16
     {512, 1, 1024, 7, 3, 1, 0, 1, 432},   // 62: as 59, with flags 16 and 32
     {512, 1, 1024, 8, 3, 1, 0, 1, 432},   // 63: as 60, with flags 16 and 32
+    {512, 1, 1024, 6, 3, 1, 0, 1, 400},   // 64: as 58, with flag 16
+    {512, 1, 1024, 6, 3, 1, 0, 1, 432},   // 65: as 58, with flags 16 and 32
+    {512, 1, 1024, 6, 3, 1, 0, 1, 392},   // 66: as 58, with flag 8
+    {512, 1, 512, 6, 3, 1, 0, 1, 384},    // 67: as 44, flags 128 and 256
+    {512, 1, 512, 6, 3, 1, 0, 1, 400},    // 68: as 67, with flag 16
+    {512, 1, 256, 6, 3, 1, 0, 1, 384},    // 69: as 45, flags 128 and 256
+    {512, 1, 256, 6, 3, 1, 0, 1, 400},    // 70: as 69, with flag 16
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
