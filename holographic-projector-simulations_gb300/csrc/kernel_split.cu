@@ -614,11 +614,13 @@ std::vector<int> split_preferences(size_t N, size_t M) {
   (void)N;
   // fewer targets than one 1024-target tile: the tensor-core builds' 512-target tiles
   // waste no more than variant 3's, then the CUDA-core model 0 on 512 and 256
-  if (M < 1024) return {34, 44, 45, 3, 4};
-  // fastest first: the tensor-core phase (pair model 3) on source tiles of 1024,
-  // 512 and 256 (measured on the 512^2 -> 1024^2 y pass: 2.93, 2.71, 2.50e12 pairs/s), then
+  if (M < 1024) return {58, 67, 45, 3, 4};
+  // fastest first: the tensor-core phase (pair model 3) on source tiles of 1024, 512 and
+  // 256 (on the 512^2 -> 1024^2 y pass, one GB300: 91.7, 98.6 and 109.3 ms; variants 58
+  // and 67 take the polynomial columns in half turns with the degree-7 sine, 2.3 % faster
+  // than 34 and 44, while on 256-source tiles that build is 1.2 % slower than 45), then
   // the CUDA-core pair models 2, 1, 0 on ever smaller tiles
-  return {34, 44, 45, 23, 13, 9, 27, 21, 16, 11, 3, 4};
+  return {58, 67, 45, 23, 13, 9, 27, 21, 16, 11, 3, 4};
 }
 
 #define HOLO_SPLIT_DISPATCH(V, CALL)                      \

@@ -153,6 +153,13 @@ def _point_sets():
     yield "10000 identical points", np.tile([[1e-4, -2e-4, 0.3]], (10000, 1))
 
 
+def _fastest_build(holo, variant):
+    """The planner's first choice: the tensor-core phase (pair model 3) on 1024-source
+    tiles."""
+    v = next(x for x in holo.variants("split32") if x["variant"] == variant)
+    return v["pair_model"] == 3 and v["source_tile"] == 1024
+
+
 @pytest.mark.parametrize("name,pts", list(_point_sets()),
                          ids=lambda x: x if isinstance(x, str) else "")
 def test_tile_orders_match_models(holo, name, pts):
@@ -186,7 +193,7 @@ def test_planner_retiles_where_hilbert_tiles_fail(holo, orc):
         info, tiling = pl.info(), pl.tiling()
         order = pl.order(0)
     assert tiling == {"sources": "packed", "targets": "packed"}, tiling
-    assert info["variant"] == 34 and info["path_error_bound_m"] <= 3.2e-13, info
+    assert _fastest_build(holo, info["variant"]) and info["path_error_bound_m"] <= 3.2e-13, info
     np.testing.assert_array_equal(order, model_order(u))
     # and the transform on those tiles meets the split path's tolerance
     rng = np.random.default_rng(5)
@@ -200,6 +207,6 @@ def test_planner_retiles_where_hilbert_tiles_fail(holo, orc):
         assert rel_l2(y[idx], ref) < 1e-5, sign
     with holo.Plan(grid(64, 10e-6, 0.35), grid(256, 7.56e-6, 0.0), "split32") as pl:
         assert pl.tiling() == {"sources": "hilbert", "targets": "hilbert"}
-        assert pl.info()["variant"] == 34
+        assert _fastest_build(holo, pl.info()["variant"])
     with holo.Plan(grid(64, 10e-6, 0.35), grid(64, 7.56e-6, 0.0), "fp64") as pl:
         assert pl.tiling() == {"sources": "none", "targets": "none"}
