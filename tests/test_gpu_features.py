@@ -387,10 +387,10 @@ def test_batched_short_source_tile_groups(holo, orc):
             planned.add(pl.info()["variant"])
         amp, phase = rng.uniform(0, 1, ns), rng.uniform(0, 2 * np.pi, ns)
         cases.append((amp, phase, u, sign))
-    tc_short = {var["variant"] for var in holo.variants("split32")
-                if var["pair_loop"] == 3 and var["source_tile"] in (256, 512)}
-    assert tc_short <= planned, (planned, "these geometries no longer select the short-tile "
-                                          "tensor-core builds")
+    tc_tiles = {var["source_tile"] for var in holo.variants("split32")
+                if var["pair_loop"] == 3 and var["variant"] in planned}
+    assert {256, 512, 1024} <= tc_tiles, (planned, "these geometries no longer select the "
+                                                   "short-tile tensor-core builds")
     probs = [holo.Problem(T(a), T(p), T(u), T(v), s, LAM,
                           torch.zeros(2 * len(v), dtype=torch.float64, device=dev))
              for a, p, u, s in cases]
