@@ -549,10 +549,6 @@ constexpr Variant kVariants[] = {
     {512, 1, 512, 6, 3, 1, 0, 1, 400},    // 68: as 67, with flag 16
     {512, 1, 256, 6, 3, 1, 0, 1, 384},    // 69: as 45, flags 128 and 256
     {512, 1, 256, 6, 3, 1, 0, 1, 400},    // 70: as 69, with flag 16
-    // build flag 512: column groups 2, 3 all on the polynomial, 0, 1 all on MUFU
-    {512, 1, 1024, 8, 3, 1, 0, 1, 896},   // 71: with flags 128 and 256
-    {512, 1, 1024, 8, 3, 1, 0, 1, 640},   // 72: with flag 128
-    {512, 1, 1024, 8, 3, 1, 0, 1, 512},   // 73: the degree-9 polynomial in radians
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 

@@ -162,12 +162,9 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
 // so the tensor cores deliver their phases in half turns and the polynomial needs no
 // multiply; kTcSin7 -- with kTcHalfTurns, a sine of degree 7 instead of 9.  Together
 // they take the FMA-pipe sin/cos from 16 to 14 lane operations per source, so more
-// source pairs can leave the XU pipe; kTcWarpSplit -- the consumer warps of the upper
-// half of the column groups take all their pairs on the polynomial and the others all
-// on MUFU (half the pairs each way; NPP0 and NPP1 are then unused), so each pipe is fed
-// by warps that never wait on the other.
+// source pairs can leave the XU pipe.
 constexpr int kTcScalar = 1, kTcHalfUnroll = 4, kTcRcp = 8, kTcPrefetch = 16, kTcSleepMma = 32,
-              kTcSleepUse = 64, kTcHalfTurns = 128, kTcSin7 = 256, kTcWarpSplit = 512;
+              kTcSleepUse = 64, kTcHalfTurns = 128, kTcSin7 = 256;
 
 // BATCHED: work items (problem, target tile, source range, split) come from a
 // device queue (atomic counter) and each names its own problem descriptor;
@@ -407,10 +404,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
               // column of row i in its block, and whether the pair loop takes its sin/cos
               // from the polynomial (source pair pp < npp of its 16-column chunk)
               const int c = (i % kTcN) % S::Cols, pp = (c % 16) / 2;
-              const bool poly_col = (FL & kTcWarpSplit)
-                                        ? (i % kTcN) / S::Cols >= CG / 2
-                                        : pp < (((c / 16) & 1) ? NPP1 : NPP0);
-              if (poly_col) {
+              if (pp < (((c / 16) & 1) ? NPP1 : NPP0)) {
                 constexpr float kInvPi = 0.318309886f;
 #pragma unroll
                 for (int k = 0; k < kTcK; ++k) g[r][k] *= kInvPi;
@@ -584,23 +578,7 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
               using Odd = std::integral_constant<int, 1>;
               using NppEven = std::integral_constant<int, NPP0>;
               using NppOdd = std::integral_constant<int, NPP1>;
-              using AllPoly = std::integral_constant<int, 8>;
-              using AllMufu = std::integral_constant<int, 0>;
-              if (FL & kTcWarpSplit) {
-                if (cg >= CG / 2) {
-#pragma unroll
-                  for (int ch = 0; ch < S::Chunks; ch += 2) {
-                    chunk(Even{}, AllPoly{}, ch);
-                    chunk(Odd{}, AllPoly{}, ch + 1);
-                  }
-                } else {
-#pragma unroll
-                  for (int ch = 0; ch < S::Chunks; ch += 2) {
-                    chunk(Even{}, AllMufu{}, ch);
-                    chunk(Odd{}, AllMufu{}, ch + 1);
-                  }
-                }
-              } else if (FL & kTcHalfUnroll) {
+              if (FL & kTcHalfUnroll) {
 #pragma unroll 1
                 for (int ch = 0; ch < S::Chunks; ch += 2) {
                   chunk(Even{}, NppEven{}, ch);
@@ -726,9 +704,6 @@ int occupancy_tc(int *out) {
   HOLO_TC_CASE(512, 3, 3, kTcHalfTurns | kTcSin7 | kTcPrefetch) \
   HOLO_TC_CASE(256, 3, 3, kTcHalfTurns | kTcSin7) \
   HOLO_TC_CASE(256, 3, 3, kTcHalfTurns | kTcSin7 | kTcPrefetch) \
-  HOLO_TC_CASE(1024, 4, 4, kTcWarpSplit | kTcHalfTurns | kTcSin7) \
-  HOLO_TC_CASE(1024, 4, 4, kTcWarpSplit | kTcHalfTurns) \
-  HOLO_TC_CASE(1024, 4, 4, kTcWarpSplit) \
   HOLO_TC_CASE(1024, 3, 4, 0)                 \
   HOLO_TC_CASE(1024, 3, 4, kTcScalar)         \
   HOLO_TC_CASE(1024, 3, 4, kTcHalfUnroll)     \
