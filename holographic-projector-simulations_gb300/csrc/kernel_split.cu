@@ -549,6 +549,8 @@ constexpr Variant kVariants[] = {
     {512, 1, 512, 6, 3, 1, 0, 1, 400},    // 68: as 67, with flag 16
     {512, 1, 256, 6, 3, 1, 0, 1, 384},    // 69: as 45, flags 128 and 256
     {512, 1, 256, 6, 3, 1, 0, 1, 400},    // 70: as 69, with flag 16
+    {512, 1, 768, 6, 3, 1, 0, 1, 384},    // 71: as 41 (24 consumer warps), flags 128 and 256
+    {512, 1, 768, 7, 3, 1, 0, 1, 384},    // 72: as 43, flags 128 and 256
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -614,13 +616,14 @@ std::vector<int> split_preferences(size_t N, size_t M) {
   (void)N;
   // fewer targets than one 1024-target tile: the tensor-core builds' 512-target tiles
   // waste no more than variant 3's, then the CUDA-core model 0 on 512 and 256
-  if (M < 1024) return {58, 67, 45, 3, 4};
-  // fastest first: the tensor-core phase (pair model 3) on source tiles of 1024, 512 and
-  // 256 (on the 512^2 -> 1024^2 y pass, one GB300: 91.7, 98.6 and 109.3 ms; variants 58
-  // and 67 take the polynomial columns in half turns with the degree-7 sine, 2.3 % faster
-  // than 34 and 44, while on 256-source tiles that build is 1.2 % slower than 45), then
-  // the CUDA-core pair models 2, 1, 0 on ever smaller tiles
-  return {58, 67, 45, 23, 13, 9, 27, 21, 16, 11, 3, 4};
+  if (M < 1024) return {58, 71, 67, 45, 3, 4};
+  // fastest first: the tensor-core phase (pair model 3) on source tiles of 1024, 768, 512
+  // and 256 (on the 512^2 -> 1024^2 y pass, one GB300: 91.7, 97.2, 98.6 and 109.3 ms;
+  // variants 58, 71 and 67 take the polynomial columns in half turns with the degree-7
+  // sine, 2.3 % faster than 34, 2.2 % than 41 and 2.3 % than 44, while on 256-source
+  // tiles that build is 1.2 % slower than 45), then the CUDA-core pair models 2, 1, 0 on
+  // ever smaller tiles
+  return {58, 71, 67, 45, 23, 13, 9, 27, 21, 16, 11, 3, 4};
 }
 
 #define HOLO_SPLIT_DISPATCH(V, CALL)                      \

@@ -704,6 +704,8 @@ int occupancy_tc(int *out) {
   HOLO_TC_CASE(512, 3, 3, kTcHalfTurns | kTcSin7 | kTcPrefetch) \
   HOLO_TC_CASE(256, 3, 3, kTcHalfTurns | kTcSin7) \
   HOLO_TC_CASE(256, 3, 3, kTcHalfTurns | kTcSin7 | kTcPrefetch) \
+  HOLO_TC_CASE(768, 3, 3, kTcHalfTurns | kTcSin7) \
+  HOLO_TC_CASE(768, 3, 4, kTcHalfTurns | kTcSin7) \
   HOLO_TC_CASE(1024, 3, 4, 0)                 \
   HOLO_TC_CASE(1024, 3, 4, kTcScalar)         \
   HOLO_TC_CASE(1024, 3, 4, kTcHalfUnroll)     \
