@@ -551,6 +551,12 @@ constexpr Variant kVariants[] = {
     {512, 1, 256, 6, 3, 1, 0, 1, 400},    // 70: as 69, with flag 16
     {512, 1, 768, 6, 3, 1, 0, 1, 384},    // 71: as 41 (24 consumer warps), flags 128 and 256
     {512, 1, 768, 7, 3, 1, 0, 1, 384},    // 72: as 43, flags 128 and 256
+    // the builder-warp kernel (flag 512; 1024: two builder warps, not four) with the
+    // half-turn polynomial: as 58, 71, 67, 69
+    {512, 1, 1024, 6, 3, 1, 0, 1, 896},   // 73
+    {512, 1, 768, 6, 3, 1, 0, 1, 896},    // 74
+    {512, 1, 512, 6, 3, 1, 0, 1, 896},    // 75
+    {512, 1, 256, 6, 3, 1, 0, 1, 1920},   // 76
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -616,14 +622,14 @@ std::vector<int> split_preferences(size_t N, size_t M) {
   (void)N;
   // fewer targets than one 1024-target tile: the tensor-core builds' 512-target tiles
   // waste no more than variant 3's, then the CUDA-core model 0 on 512 and 256
-  if (M < 1024) return {58, 71, 67, 45, 3, 4};
-  // fastest first: the tensor-core phase (pair model 3) on source tiles of 1024, 768, 512
-  // and 256 (on the 512^2 -> 1024^2 y pass, one GB300: 91.7, 97.2, 98.6 and 109.3 ms;
-  // variants 58, 71 and 67 take the polynomial columns in half turns with the degree-7
-  // sine, 2.3 % faster than 34, 2.2 % than 41 and 2.3 % than 44, while on 256-source
-  // tiles that build is 1.2 % slower than 45), then the CUDA-core pair models 2, 1, 0 on
-  // ever smaller tiles
-  return {58, 71, 67, 45, 23, 13, 9, 27, 21, 16, 11, 3, 4};
+  if (M < 1024) return {73, 75, 76, 3, 4};
+  // fastest first: the tensor-core phase (pair model 3) in the builder-warp kernel on
+  // source tiles of 1024, 512 and 256 (on the 512^2 -> 1024^2 y pass, one GB300: 90.8,
+  // 94.6 and 99.0 ms, against 91.8, 98.5 and 110.7 ms for the same tiles with the operands
+  // built between tile pairs, variants 58, 67 and 69; 768-source tiles, 71 at 97.0 ms,
+  // are slower than 512 and their bound wider, so they never come first), then the
+  // CUDA-core pair models 2, 1, 0 on ever smaller tiles
+  return {73, 75, 76, 23, 13, 9, 27, 21, 16, 11, 3, 4};
 }
 
 #define HOLO_SPLIT_DISPATCH(V, CALL)                      \
