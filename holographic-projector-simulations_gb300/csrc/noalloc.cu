@@ -23,8 +23,9 @@
 //   - input and output pointers must be memory of `device` (or managed
 //     memory): the path enables no peer access;
 //   - the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (with that device current); make that first call
-//     before any stream capture.
+//     cudaGetSymbolAddress (with that device current);
+//   - a call waits for its stream partway (the tile statistics are read back), so a
+//     stream being captured into a graph is refused with HOLO_ERR_INVALID.
 //   - no cudaMalloc, cudaFree, memory-pool or allocating library routine is
 //     called on this path.
 #include <math.h>
@@ -169,6 +170,14 @@ struct DrainOnReturn {
 int transform_noalloc(int device, int sign, double lambda, const double *amp,
                       const double *phase, const double *u, size_t N, const double *v,
                       size_t M, double *y, cudaStream_t s) {
+  // the call reads the tile statistics back and waits for its stream partway, which a
+  // stream being captured into a graph does not allow: refuse before queuing anything
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  HOLO_CUDA(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(HOLO_ERR_INVALID,
+                "holo_transform_noalloc waits for its stream partway and cannot be captured "
+                "into a graph");
   if (sign != 1 && sign != -1) return fail(HOLO_ERR_INVALID, "sign must be +1 or -1 (got %d)", sign);
   if (!(lambda > 0.0) || !isfinite(lambda)) return fail(HOLO_ERR_INVALID, "lambda must be finite and > 0");
   if ((N && (!amp || !phase || !u)) || (M && (!v || !y)))

@@ -276,8 +276,9 @@ int holo_selftest_bounded_wait(holo_handle h, long long max_cycles, holo_stream_
  * HOLO_ERR_INVALID.  Every call shares that array and overwrites it, so calls
  * that overlap on the GPU race: calls in one process are serialised by a lock
  * and each returns only after its work on `stream` has finished.  The first
- * call on a device looks up the array's address (cudaGetSymbolAddress); make
- * it before any stream capture. */
+ * call on a device looks up the array's address (cudaGetSymbolAddress).  A
+ * call waits for `stream` partway (it reads the tile statistics back), so a
+ * stream being captured into a graph is refused with HOLO_ERR_INVALID. */
 int holo_transform_noalloc(int device, int sign, double lambda, const double *amp,
                            const double *phase, const double *u_xyz, size_t N,
                            const double *v_xyz, size_t M, double *y_re_im,

@@ -82,3 +82,26 @@ def test_noalloc_rejects_memory_of_another_device(holo):
                                     small.data_ptr(), 1, small.data_ptr(), 1, small.data_ptr(),
                                     None)
     assert rc == -1 and b"device pointers of device 1" in lib.holo_last_error_string()
+
+
+def test_noalloc_refuses_a_stream_under_capture(holo):
+    """The call waits for its stream partway, so a stream being captured into a graph is
+    refused before anything is queued (the capture then ends empty)."""
+    import torch
+    lib = holo._native.load()
+    dev = torch.device("cuda:0")
+    amp, phase, u, v, _ = chain64(0)
+    v = v[:4096]
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device=dev)
+    ta, tp, tu, tv = T(amp), T(phase), T(u), T(v)
+    y = torch.zeros(2 * len(v), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream(dev)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        rc = _call(lib, ta, tp, tu, tv, -1, y, s.cuda_stream)
+    assert rc == -1 and b"captured" in lib.holo_last_error_string()
+    # the stream is usable afterwards: the same call outside the capture succeeds
+    rc = _call(lib, ta, tp, tu, tv, -1, y, torch.cuda.current_stream(dev).cuda_stream)
+    assert rc == 0, lib.holo_last_error_string()
+    assert torch.count_nonzero(y).item() > 0
