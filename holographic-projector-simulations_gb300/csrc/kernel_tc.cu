@@ -683,8 +683,9 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
 }
 
 // ---- builder-warp kernel (kTcBuilders) -----------------------------------------------------
-// The same tile pairs and pair loop, with the operands built by warps of their own
-// while the consumers sum: the consumers never stop for a build, a frame or a carry.
+// The same tile pairs and pair loop as k_split_tc, with the operands built by warps of
+// their own while the consumers sum: the consumers never stop for a build, a frame or a
+// carry.
 // Blocks run source block outer (n), target block inner (m), so that source block n is
 // free for the next tile pair once the MMAs of (3, n) are complete, a quarter tile
 // after it was built, and the next tile pair's target rows go to a second buffer (the
@@ -693,8 +694,8 @@ __global__ void __launch_bounds__(TcShape<CG, NBLK>::Threads, 1)
 // shared memory.  The builders read the source records from global memory (they stay
 // in L2), carry each tile pair's partial sums into the running sums two tile pairs
 // later, and write the item's results.  Hand-offs, one phase per tile pair q:
-//   opa_ready[q & 1]   target rows of q built (64 builder arrivals)       -> MMA warp
-//   opb_ready[n]       source block n of q built (64)                      -> MMA warp,
+//   opa_ready[q & 1]   target rows of q built (one arrival per builder thread) -> MMA warp
+//   opb_ready[n]       source block n of q built (the same)                -> MMA warp,
 //                      and for the consumers, that block's amplitudes
 //   opb_free[n]        the MMAs of (3, n) of q are complete (tcgen05.commit) -> builders
 //   tile_done[q & 1]   every MMA of q is complete (tcgen05.commit)         -> builders
@@ -724,8 +725,8 @@ struct TcBwSmem {
   static constexpr size_t tph = acc + kTcTT * 16;                      // float [2][TT]
   static constexpr size_t tsc = tph + 2 * kTcTT * 4;                   // float [2][TT]
   static constexpr size_t frame = tsc + 2 * kTcTT * 4;                 // Frame [2]
-  static constexpr int kBars = 26;
-  static constexpr size_t bars = (frame + 2 * sizeof(Frame) + 15) / 16 * 16;  // uint64 [26]
+  static constexpr int kBars = 22;
+  static constexpr size_t bars = (frame + 2 * sizeof(Frame) + 15) / 16 * 16;  // uint64 [22]
   static constexpr size_t misc = bars + kBars * 8;                     // uint32 taddr, abort
   static constexpr size_t bytes = misc + 16;
 };
