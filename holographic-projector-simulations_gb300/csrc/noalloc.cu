@@ -23,7 +23,9 @@
 //   - input and output pointers must be memory of `device` (or managed
 //     memory): the path enables no peer access;
 //   - the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (with that device current);
+//     cudaGetSymbolAddress (with that device current) and keeps it for the life of the
+//     process; a cudaDeviceReset may move the array, after which this path must not be
+//     used again in the process;
 //   - a call waits for its stream partway (the tile statistics are read back), so a
 //     stream being captured into a graph is refused with HOLO_ERR_INVALID.
 //   - no cudaMalloc, cudaFree, memory-pool or allocating library routine is

@@ -276,7 +276,9 @@ int holo_selftest_bounded_wait(holo_handle h, long long max_cycles, holo_stream_
  * HOLO_ERR_INVALID.  Every call shares that array and overwrites it, so calls
  * that overlap on the GPU race: calls in one process are serialised by a lock
  * and each returns only after its work on `stream` has finished.  The first
- * call on a device looks up the array's address (cudaGetSymbolAddress).  A
+ * call on a device looks up the array's address (cudaGetSymbolAddress) and keeps
+ * it for the life of the process: after a cudaDeviceReset, which may move the
+ * array, this entry point must not be called again in that process.  A
  * call waits for `stream` partway (it reads the tile statistics back), so a
  * stream being captured into a graph is refused with HOLO_ERR_INVALID. */
 int holo_transform_noalloc(int device, int sign, double lambda, const double *amp,
